@@ -1,0 +1,340 @@
+"""Benchmark of the bit-serial GEMM hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+A step is one gemmBitSerial over one pair of packed operands: by default the
+2048 x 4096 x 2048 GEMM of a 3-bit unsigned lhs with a 2-bit signed rhs.  The
+metric is the reference's GOPS = 2*M*K*N / time (benchmark/benchmark.cpp:107).
+
+* value: inputs already packed in HBM; each step's forward kernel is timed
+  with CUDA events on the launching stream; L2 is flushed (256 MiB write,
+  outside the events) before every step.
+* e2e: the same metric through the C ABI from pinned HOST buffers: both
+  imports (host->device copy + pack), the GEMM and the result read-back.
+* roofline: the forward kernel's AND+popcount rate against the CUDA-core POPC
+  pipe's measured peak (gbs_pipe_peaks, run in this process).
+* cpu_baseline: the reference's algorithm on this host's cores (the compiled
+  reference when present, else the oracle's C restatement), same workload.
+
+--impl reference times that CPU implementation alone, as the reference arm.
+With N > 1 GPUs (torchrun) every rank runs an independent replica.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import hashlib
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bit-exact GOPS @2048x4096x2048 w3/w2; grouped & adjoint speedup vs plain GPU"
+DEFAULT_WORKLOAD = "gemm_2048x4096x2048_u3s2"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default=DEFAULT_WORKLOAD)
+    p.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload_desc(name):
+    from gemmbitserial_gb300 import datagen
+    M, K, N, (wA, eA), (wB, eB) = datagen.WORKLOADS[name]
+    return {"workload": name, "M": M, "K": K, "N": N, "lhs": f"{eA}{wA}", "rhs": f"{eB}{wB}",
+            "rhs_layout": "transposed (N x K)", "result_layout": "transposed (N x M) int32"}
+
+
+def gops(M, K, N, seconds):
+    return 2.0 * M * K * N / seconds / 1e9
+
+
+# ---------------------------------------------------------------- CPU side
+
+def cpu_time(name, seconds_budget, threads, max_reps=1000):
+    """Times the reference's gemmBitSerial on the host (imports untimed). Returns (sec/call, kind, sample)."""
+    from gemmbitserial_gb300 import datagen
+    from oracle import oracle as O
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+    if O.ref_available():
+        R = O.ref()
+        t1 = R.ref_time_gemm(M, K, N, wA, wB, int(sA), int(sB), O._ptr(A), O.DT_I8, O._ptr(B), O.DT_I8, 1, threads, None)
+        reps = int(max(1, min(max_reps, seconds_budget / max(t1, 1e-6))))
+        t = R.ref_time_gemm(M, K, N, wA, wB, int(sA), int(sB), O._ptr(A), O.DT_I8, O._ptr(B), O.DT_I8, reps, threads, None)
+        return t, "reference", f"full {M}x{K}x{N} GEMM, {reps} timed calls after 1 warm-up, {threads} threads (rhs rows split)"
+    ctx = O.OracleContext(M, K, N, wA, wB, sA, sB)
+    ctx.import_(0, A)
+    ctx.import_(1, B)
+    ctx.gemm(threads)  # warm-up
+    t0 = time.perf_counter()
+    ctx.gemm(threads)
+    t1 = time.perf_counter() - t0
+    reps = int(max(1, min(max_reps, seconds_budget / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.gemm(threads)
+    t = (time.perf_counter() - t0) / reps
+    ctx.close()
+    return t, "port", f"full {M}x{K}x{N} GEMM, {reps} timed calls after 1 warm-up, {threads} threads (rhs rows split)"
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    desc = workload_desc(args.workload)
+    M, K, N = desc["M"], desc["K"], desc["N"]
+    threads = os.cpu_count() or 1
+    from gemmbitserial_gb300 import datagen
+    from oracle import oracle as O
+    _, _, _, wA, sA, wB, sB, A, B = datagen.workload(args.workload)
+    if O.ref_available():
+        R = O.ref()
+        R.ref_time_gemm(M, K, N, wA, wB, int(sA), int(sB), O._ptr(A), O.DT_I8, O._ptr(B), O.DT_I8, args.warmup, threads, None)
+        sec = R.ref_time_gemm(M, K, N, wA, wB, int(sA), int(sB), O._ptr(A), O.DT_I8, O._ptr(B), O.DT_I8, args.steps, threads, None)
+        kind = "reference"
+    else:
+        ctx = O.OracleContext(M, K, N, wA, wB, sA, sB)
+        ctx.import_(0, A)
+        ctx.import_(1, B)
+        for _ in range(max(1, args.warmup)):
+            ctx.gemm(threads)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.gemm(threads)
+        sec = (time.perf_counter() - t0) / max(1, args.steps)
+        ctx.close()
+        kind = "port"
+    v = gops(M, K, N, sec)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "GOPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded splitmix64)", "config": dict(desc, parallelism="host threads"),
+            "cpu_baseline": {"value": round(v, 3), "unit": "GOPS", "cores": threads, "kind": kind,
+                             "sample": f"full {M}x{K}x{N} gemmBitSerial per step, imports untimed, rhs rows split over {threads} threads"},
+            "e2e": {"value": round(v, 3), "unit": "GOPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def read_traffic(kernel, workload):
+    """dram bytes per launch recorded from an ncu capture (profiles/ncu_<kernel>_<workload>.txt)."""
+    path = os.path.join(ROOT, "profiles", f"ncu_{kernel}_{workload}.txt")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from gemmbitserial_gb300 import _capi, datagen
+    from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext
+    lib = _capi.load()
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload(args.workload)
+    desc = workload_desc(args.workload)
+    stream = torch.cuda.Stream(device=dev)
+    sh = C.c_void_p(stream.cuda_stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- resident path: packed operands in HBM
+    ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    dA = torch.from_numpy(A).to(dev)
+    dB = torch.from_numpy(B).to(dev)
+    with torch.cuda.stream(stream):
+        ctx.lhs.importRegular(dA, stream=stream)
+        ctx.rhs.importRegular(dB, stream=stream)
+    stream.synchronize()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            _capi.check(lib.gbs_gemm(ctx._h, sh))
+    barrier()
+    launches0 = lib.gbs_debug_launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                flush.zero_()
+                ev[i][0].record(stream)
+                _capi.check(lib.gbs_gemm(ctx._h, sh))
+                ev[i][1].record(stream)
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    launches = lib.gbs_debug_launch_count() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    res = ctx.res.reshape(N, M)
+    want = json.load(open(os.path.join(ROOT, "tests", "golden", "ref_configs.json"))).get(args.workload, {}).get("sha256")
+    got = hashlib.sha256(np.ascontiguousarray(res).tobytes()).hexdigest()
+    parity = "bit-exact vs reference (sha256)" if got == want else ("MISMATCH" if want else "unchecked")
+    pipe = ctx.pipe
+    deallocGEMMContext(ctx)
+
+    # ---- end to end through the C ABI from pinned host buffers
+    hA = torch.from_numpy(A).pin_memory()
+    hB = torch.from_numpy(B).pin_memory()
+    hR = torch.empty(M * N, dtype=torch.int32).pin_memory()
+    ctx2 = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+
+    def e2e_step():
+        _capi.check(lib.gbs_import(ctx2._h, 0, C.c_void_p(hA.data_ptr()), _capi.GBS_I8, 0, sh))
+        _capi.check(lib.gbs_import(ctx2._h, 1, C.c_void_p(hB.data_ptr()), _capi.GBS_I8, 0, sh))
+        _capi.check(lib.gbs_gemm(ctx2._h, sh))
+        _capi.check(lib.gbs_get_result(ctx2._h, C.c_void_p(hR.data_ptr()), sh))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_ok = hashlib.sha256(hR.numpy().tobytes()).hexdigest() == want
+    deallocGEMMContext(ctx2)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    if rank != 0:
+        return
+    # ---- roofline of the forward kernel against the measured POPC pipe peak
+    popc, bmma = C.c_double(), C.c_double()
+    _capi.check(lib.gbs_pipe_peaks(C.byref(popc), C.byref(bmma)))
+    kpad = (K + 63) // 64 * 64
+    binops = 2.0 * M * N * kpad * wA * wB  # AND + add per bit of each plane pair
+    achieved = binops / (ms * 1e-3) / 1e12
+    peak = 2.0 * popc.value / 1e12
+    kernel = "gemm_popc_tiled"
+    traffic = read_traffic(kernel, args.workload)
+    clocks = clk.summary()
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        threads = os.cpu_count() or 1
+        sec, kind, sample = cpu_time(args.workload, args.cpu_seconds, threads)
+        cpu = {"value": round(gops(M, K, N, sec), 3), "unit": "GOPS", "cores": threads, "kind": kind, "sample": sample}
+
+    v = gops(M, K, N, ms * 1e-3) * world
+    line = {"metric": METRIC, "value": round(v, 3), "unit": "GOPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded splitmix64)",
+            "config": dict(desc, parallelism=f"replicas x{world}", l2="flushed before every step (256 MiB write, outside the timed events)",
+                           pipe={1: "popc", 2: "bmma"}.get(pipe, str(pipe))),
+            "parity": parity,
+            "e2e": {"value": round(gops(M, K, N, e2e_s) * world, 3), "unit": "GOPS",
+                    "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),
+                    "ms_per_step": round(e2e_s * 1e3, 4), "parity": "bit-exact" if e2e_ok else "MISMATCH"},
+            "roofline": {"bound": "popc", "kernel": kernel, "achieved": round(achieved, 3), "peak": round(peak, 3),
+                         "unit": "Tbinop/s", "frac": round(achieved / peak, 4),
+                         "peak_source": "measured in-process (gbs_pipe_peaks: CUDA-core AND+POPC loop)",
+                         "bmma_peak": round(2.0 * bmma.value / 1e12, 3),
+                         "traffic": traffic, "algorithmic_bytes": int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)},
+            "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
+            "wall_s_timed_region": round(t_wall, 4)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    world, _, _ = dist_env()
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

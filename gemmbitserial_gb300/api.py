@@ -1,0 +1,206 @@
+"""Python mirror of gemmbitserial's public API over the C ABI.
+
+Same names, argument meaning and error behaviour as the reference's hot path
+(gemmbitserial.hpp:379-479, arch-generic.hpp:78-100, 331-345):
+
+    ctx = allocGEMMContext(M, K, N, lhsBits, rhsBits, lhsSigned, rhsSigned)
+    ctx.lhs.importRegular(A)          # M x K
+    ctx.rhs.importRegular(BT)         # N x K (B transposed)
+    gemmBitSerial(ctx)
+    res = ctx.res                     # N*M int32, transposed result
+    deallocGEMMContext(ctx)
+
+All compute runs in libgbs.so on the GPU.  Inputs may be numpy arrays (host)
+or torch CUDA tensors (device).  Integer element types select the reference's
+import overload: uint8 is the raw-bit overload (gemmbitserial.hpp:249), the
+signed types go through quantize<T> (gemmbitserial.hpp:170).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+
+_NP2DT = {np.dtype(np.int8): _capi.GBS_I8, np.dtype(np.uint8): _capi.GBS_U8,
+          np.dtype(np.int16): _capi.GBS_I16, np.dtype(np.int32): _capi.GBS_I32}
+
+
+def _stream_handle(stream):
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        except ImportError:
+            pass
+        return C.c_void_p(0)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _src(arr):
+    """(pointer, dtype code, keepalive) for a numpy array or torch tensor."""
+    try:
+        import torch
+        if isinstance(arr, torch.Tensor):
+            t = arr.contiguous()
+            dt = {torch.int8: _capi.GBS_I8, torch.uint8: _capi.GBS_U8,
+                  torch.int16: _capi.GBS_I16, torch.int32: _capi.GBS_I32}[t.dtype]
+            return C.c_void_p(t.data_ptr()), dt, t
+    except ImportError:
+        pass
+    a = np.ascontiguousarray(arr)
+    if a.dtype not in _NP2DT:
+        raise TypeError(f"unsupported element type {a.dtype}; use int8, uint8, int16 or int32")
+    return C.c_void_p(a.ctypes.data), _NP2DT[a.dtype], a
+
+
+class BitSerialMatrix:
+    """One operand of a context (gemmbitserial.hpp:19-50); the planes live on the GPU."""
+
+    def __init__(self, ctx: "GEMMContext", side: int):
+        self._ctx = ctx
+        self._side = side
+
+    def _info(self):
+        i = self._ctx._info()
+        return i.rhs if self._side else i.lhs
+
+    @property
+    def nbits(self): return self._info().nbits
+
+    @property
+    def nrows(self): return self._info().nrows
+
+    @property
+    def ncols(self): return self._info().ncols
+
+    @property
+    def nrows_a(self): return self._info().nrows_a
+
+    @property
+    def ncols_a(self): return self._info().ncols_a
+
+    @property
+    def issigned(self): return bool(self._info().issigned)
+
+    @property
+    def data(self):
+        """Device address of the planes, layout [nbits][nrows_a][ncols_a/64] of uint64."""
+        return self._info().data
+
+    def isBipolar(self) -> bool:
+        return bool(self._info().isbipolar)
+
+    def wordsPerRow(self) -> int:
+        return self.ncols_a // 64
+
+    def wordsPerBitplane(self) -> int:
+        return self.nrows_a * self.wordsPerRow()
+
+    def importRegular(self, matrix, readColMajor: bool = False, stream=None) -> None:
+        """importRegular<T> / importRegular(uint8_t*) (gemmbitserial.hpp:213, 249)."""
+        ptr, dt, keep = _src(matrix)
+        _capi.check(_capi.load().gbs_import(self._ctx._h, self._side, ptr, dt, int(bool(readColMajor)),
+                                            _stream_handle(stream)))
+        del keep
+
+    def planes(self, stream=None) -> np.ndarray:
+        """Host copy of the packed planes, shape [nbits, nrows_a, ncols_a/64] (uint64)."""
+        i = self._info()
+        shape = (int(i.nbits), int(i.nrows_a), int(i.ncols_a // 64))
+        out = np.zeros(max(int(np.prod(shape)), 1), np.uint64)
+        _capi.check(_capi.load().gbs_get_planes(self._ctx._h, self._side, C.c_void_p(out.ctypes.data),
+                                                _stream_handle(stream)))
+        return out[:int(np.prod(shape))].reshape(shape)
+
+    def exportRegular(self, stream=None) -> np.ndarray:
+        """exportRegular<int32_t> (gemmbitserial.hpp:313-333): rows x ncols int32 on the host."""
+        out = np.zeros(max(self.nrows * self.ncols, 1), np.int32)
+        _capi.check(_capi.load().gbs_export(self._ctx._h, self._side, C.c_void_p(out.ctypes.data),
+                                            _stream_handle(stream)))
+        return out[:self.nrows * self.ncols].reshape(self.nrows, self.ncols)
+
+
+class GEMMContext:
+    """GEMMContext (gemmbitserial.hpp:379-411).  Copies of the Python object share one context."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self.lhs = BitSerialMatrix(self, 0)
+        self.rhs = BitSerialMatrix(self, 1)
+
+    def _info(self):
+        if not self._h:
+            raise RuntimeError("context has been deallocated")
+        info = _capi.CtxInfo()
+        _capi.check(_capi.load().gbs_ctx_get_info(self._h, C.byref(info)))
+        return info
+
+    @property
+    def lhsBlock(self): return self._info().lhsBlock
+
+    @property
+    def rhsBlock(self): return self._info().rhsBlock
+
+    @property
+    def res(self) -> np.ndarray:
+        """ctx.res: the rhs.nrows x lhs.nrows int32 result, flattened (transposed layout)."""
+        info = self._info()
+        n = info.lhs.nrows * info.rhs.nrows
+        out = np.zeros(max(n, 1), np.int32)
+        _capi.check(_capi.load().gbs_get_result(self._h, C.c_void_p(out.ctypes.data), _stream_handle(None)))
+        return out[:n]
+
+    @property
+    def res_device(self) -> int:
+        return self._info().res
+
+    def isBipolarTimesRegular(self) -> bool:
+        return self.lhs.isBipolar() != self.rhs.isBipolar()
+
+    def isBipolarTimesBipolar(self) -> bool:
+        return self.lhs.isBipolar() and self.rhs.isBipolar()
+
+    def isMatrixVector(self) -> bool:
+        return self.rhs.nrows == 1
+
+    def set_pipe(self, pipe: int) -> None:
+        _capi.check(_capi.load().gbs_set_pipe(self._h, pipe))
+
+    @property
+    def pipe(self) -> int:
+        return self._info().pipe
+
+
+def allocGEMMContext(lhsRows, depth, rhsRows, lhsBits, rhsBits, lhsSigned, rhsSigned) -> GEMMContext:
+    """allocGEMMContext (arch-generic.hpp:78-100, gemmbitserial.hpp:415-452)."""
+    h = C.c_void_p()
+    _capi.check(_capi.load().gbs_ctx_alloc(int(lhsRows), int(depth), int(rhsRows), int(lhsBits), int(rhsBits),
+                                           int(bool(lhsSigned)), int(bool(rhsSigned)), C.byref(h)))
+    return GEMMContext(h)
+
+
+allocateGEMMContext = allocGEMMContext  # the name README.md:15 uses
+
+
+def gemmBitSerial(ctx: GEMMContext, stream=None) -> None:
+    """gemmBitSerial (arch-generic.hpp:331-345); asynchronous on the stream."""
+    _capi.check(_capi.load().gbs_gemm(ctx._h, _stream_handle(stream)))
+
+
+def deallocGEMMContext(ctx: GEMMContext) -> None:
+    """deallocGEMMContext (gemmbitserial.hpp:454-458)."""
+    if ctx._h:
+        _capi.check(_capi.load().gbs_ctx_free(ctx._h))
+        ctx._h = None
+
+
+def sumRows(m: BitSerialMatrix, stream=None) -> np.ndarray:
+    """sumRows (arch-generic.hpp:6-37): per-row sum of the values of one operand."""
+    out = np.zeros(max(m.nrows, 1), np.int32)
+    _capi.check(_capi.load().gbs_sum_rows(m._ctx._h, m._side, C.c_void_p(out.ctypes.data), _stream_handle(stream)))
+    return out[:m.nrows]

@@ -1,0 +1,369 @@
+// gbs_api.cu -- the C ABI declared in include/gbs.h.
+//
+// Host-side control of the bit-serial GEMM path: context allocation and
+// sizing (allocGEMMContext_base, gemmbitserial.hpp:415-452), imports
+// (importRegular, :213-275), the forward dispatch (gemmBitSerial_generic,
+// arch-generic.hpp:331-345) with its encoding-dependent epilogue
+// (prepareAccumulators_generic, :39-76; usingBinary weights, :179-192;
+// bipolar correction, :255-259), result read-back and deallocation.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "gbs_internal.h"
+
+namespace gbs {
+
+static thread_local std::string g_last_error;
+static std::atomic<int> g_fail_alloc_countdown{0};
+static std::atomic<uint64_t> g_launches{0};
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return GBS_ECUDA;
+}
+
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+cudaError_t dev_alloc(void **p, size_t bytes) {
+  int c = g_fail_alloc_countdown.load();
+  if (c > 0) {
+    if (g_fail_alloc_countdown.fetch_sub(1) == 1) {
+      *p = nullptr;
+      return cudaErrorMemoryAllocation;
+    }
+  }
+  if (bytes == 0) bytes = 256;
+  return cudaMalloc(p, bytes);
+}
+
+namespace {
+
+uint64_t round_up(uint64_t x, uint64_t a) { return a ? (x + a - 1) / a * a : x; }
+
+// Makes the context's device current for the scope of one call.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) { ok = false; return; }
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+  }
+  ~DeviceGuard() {
+    int cur;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+bool is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the sticky-free error of an unknown host pointer
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+size_t elem_size(int dtype) { return dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1; }
+
+void free_ctx_buffers(gbs_ctx *c) {
+  if (c->lhs.planes) cudaFree(c->lhs.planes);
+  if (c->rhs.planes) cudaFree(c->rhs.planes);
+  if (c->res) cudaFree(c->res);
+  if (c->rowsum) cudaFree(c->rowsum);
+  if (c->stage) cudaFree(c->stage);
+}
+
+// Epilogue and operand order for one context (see gbs_internal.h: Epilogue).
+void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum) {
+  memset(&e, 0, sizeof(e));
+  const bool lb = c->lhs.bipolar(), rb = c->rhs.bipolar();
+  if (lb && rb) {  // arch-generic.hpp:255-259: ncols - 2 * popc(a ^ b)
+    e.use_xor = 1;
+    e.alpha[0][0] = -2;
+    e.c0 = (uint32_t)c->lhs.ncols;
+    return;
+  }
+  const bool mixed = lb != rb;  // arch-generic.hpp:185: alpha doubled, res seeded with -rowsum(regular)
+  for (uint64_t i = 0; i < c->lhs.nbits; i++) {
+    const bool ni = c->lhs.issigned && !lb && i == c->lhs.nbits - 1;
+    for (uint64_t j = 0; j < c->rhs.nbits; j++) {
+      const bool nj = c->rhs.issigned && !rb && j == c->rhs.nbits - 1;
+      uint32_t a = 1u << (i + j);
+      if (ni != nj) a = 0u - a;
+      if (mixed) a *= 2u;
+      e.alpha[i][j] = (int32_t)a;
+    }
+  }
+  if (mixed) {
+    if (lb) e.rb = rowsum;  // result row n is seeded with -rowsum(rhs row n)
+    else e.ra = rowsum;     // result column m is seeded with -rowsum(lhs row m)
+  }
+}
+
+}  // namespace
+
+int choose_pipe(const gbs_ctx *c);
+
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" {
+
+const char *gbs_version(void) { return "gemmbitserial-gb300 0.1 (sm_103a)"; }
+
+const char *gbs_last_error(void) { return g_last_error.c_str(); }
+
+void gbs_debug_fail_alloc_after(int n) { g_fail_alloc_countdown.store(n > 0 ? n : 0); }
+
+uint64_t gbs_debug_launch_count(void) { return g_launches.load(); }
+
+int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB,
+                  gbs_ctx **out) {
+  if (!out) return fail(GBS_EINVAL, "gbs_ctx_alloc: out is NULL");
+  *out = nullptr;
+  if (wA < 1 || wA > (uint64_t)kMaxBits || wB < 1 || wB > (uint64_t)kMaxBits)
+    return fail(GBS_EINVAL, "gbs_ctx_alloc: bit widths must be in [1, 8], got " + std::to_string(wA) +
+                                " and " + std::to_string(wB));
+  if (M > (1ull << 31) || N > (1ull << 31) || K > (1ull << 31) || M * N > (1ull << 40))
+    return fail(GBS_EINVAL, "gbs_ctx_alloc: shape too large");
+  gbs_ctx *c = new gbs_ctx();
+  if (cudaGetDevice(&c->device) != cudaSuccess) {
+    delete c;
+    return cuda_fail(cudaGetLastError(), "gbs_ctx_alloc: no CUDA device");
+  }
+  auto init = [&](Mat &m, uint64_t bits, uint64_t rows, int sgn) {
+    m.nbits = bits;
+    m.nrows = rows;
+    m.ncols = K;
+    m.issigned = sgn ? 1 : 0;
+    m.nrows_a = round_up(rows, kRowAlign);
+    m.ncols_a = round_up(K, kColAlign);
+  };
+  init(c->lhs, wA, M, sA);
+  init(c->rhs, wB, N, sB);
+  c->lhsBlock = c->lhs.nrows_a ? kRowAlign : 0;
+  c->rhsBlock = c->rhs.nrows_a ? kRowAlign : 0;
+  cudaError_t e = cudaSuccess;
+  const char *what = "";
+  if (e == cudaSuccess) { what = "lhs planes"; e = dev_alloc((void **)&c->lhs.planes, c->lhs.words() * 8); }
+  if (e == cudaSuccess) { what = "rhs planes"; e = dev_alloc((void **)&c->rhs.planes, c->rhs.words() * 8); }
+  if (e == cudaSuccess) { what = "result"; e = dev_alloc((void **)&c->res, M * N * 4); }
+  if (e == cudaSuccess) { what = "row sums"; e = dev_alloc((void **)&c->rowsum, (M > N ? M : N) * 4); }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    free_ctx_buffers(c);
+    delete c;
+    return fail(GBS_ENOMEM, std::string("gbs_ctx_alloc: device allocation failed (") + what + ")");
+  }
+  // Planes start zeroed so that a context is well defined even before import.
+  cudaMemset(c->lhs.planes, 0, c->lhs.words() * 8);
+  cudaMemset(c->rhs.planes, 0, c->rhs.words() * 8);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    free_ctx_buffers(c);
+    delete c;
+    return cuda_fail(e, "gbs_ctx_alloc");
+  }
+  *out = c;
+  return GBS_OK;
+}
+
+int gbs_ctx_allocate(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB,
+                     gbs_ctx **out) {
+  return gbs_ctx_alloc(M, K, N, wA, wB, sA, sB, out);
+}
+
+int gbs_ctx_free(gbs_ctx *c) {
+  if (!c) return GBS_OK;
+  DeviceGuard g(c->device);
+  cudaDeviceSynchronize();
+  free_ctx_buffers(c);
+  delete c;
+  return GBS_OK;
+}
+
+int gbs_ctx_get_info(const gbs_ctx *c, gbs_ctx_info *info) {
+  if (!c || !info) return fail(GBS_EINVAL, "gbs_ctx_get_info: NULL argument");
+  auto fill = [](const Mat &m, gbs_matrix_info &o) {
+    o.nbits = m.nbits;
+    o.nrows = m.nrows;
+    o.ncols = m.ncols;
+    o.nrows_a = m.nrows_a;
+    o.ncols_a = m.ncols_a;
+    o.issigned = m.issigned;
+    o.isbipolar = m.bipolar() ? 1 : 0;
+    o.data = m.planes;
+  };
+  fill(c->lhs, info->lhs);
+  fill(c->rhs, info->rhs);
+  info->lhsBlock = c->lhsBlock;
+  info->rhsBlock = c->rhsBlock;
+  info->res = c->res;
+  info->pipe = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
+  return GBS_OK;
+}
+
+int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_import: ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_import: side must be 0 (lhs) or 1 (rhs)");
+  if (dtype < GBS_I8 || dtype > GBS_I32) return fail(GBS_EINVAL, "gbs_import: unknown dtype");
+  Mat &m = side ? c->rhs : c->lhs;
+  const uint64_t n = m.nrows * m.ncols;
+  if (n && !src) return fail(GBS_EINVAL, "gbs_import: src is NULL");
+  DeviceGuard g(c->device);
+  if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_import: cudaSetDevice");
+  cudaStream_t s = as_stream(stream);
+  const void *dsrc = src;
+  if (n && !is_device_ptr(src)) {
+    const size_t bytes = n * elem_size(dtype);
+    if (c->stage_bytes < bytes) {
+      cudaError_t se = cudaStreamSynchronize(s);  // the old staging buffer may still be read
+      if (se != cudaSuccess) return cuda_fail(se, "gbs_import: stream sync");
+      if (c->stage) cudaFree(c->stage);
+      c->stage = nullptr;
+      c->stage_bytes = 0;
+      if (dev_alloc(&c->stage, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GBS_ENOMEM, "gbs_import: staging allocation failed");
+      }
+      c->stage_bytes = bytes;
+    }
+    cudaError_t ce = cudaMemcpyAsync(c->stage, src, bytes, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "gbs_import: host-to-device copy");
+    dsrc = c->stage;
+    cudaError_t pe = launch_pack(m, dsrc, dtype, col_major, s);
+    if (pe != cudaSuccess) return cuda_fail(pe, "gbs_import: pack kernel");
+    // Host memory may be reused once the copy has been consumed.
+    ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "gbs_import: stream sync");
+  } else {
+    cudaError_t pe = launch_pack(m, dsrc, dtype, col_major, s);
+    if (pe != cudaSuccess) return cuda_fail(pe, "gbs_import: pack kernel");
+  }
+  m.imported = true;
+  return GBS_OK;
+}
+
+int gbs_set_pipe(gbs_ctx *c, int pipe) {
+  if (!c) return fail(GBS_EINVAL, "gbs_set_pipe: ctx is NULL");
+  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_BMMA) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
+  c->pipe = pipe;
+  return GBS_OK;
+}
+
+int gbs_gemm(gbs_ctx *c, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_gemm: ctx is NULL");
+  if (c->lhs.ncols != c->rhs.ncols) return fail(GBS_EINVAL, "gbs_gemm: lhs/rhs depth mismatch");
+  if (!c->lhs.imported || !c->rhs.imported)
+    return fail(GBS_ESTATE, "gbs_gemm: import both lhs and rhs before gemm");
+  DeviceGuard g(c->device);
+  if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_gemm: cudaSetDevice");
+  cudaStream_t s = as_stream(stream);
+  const uint64_t M = c->lhs.nrows, N = c->rhs.nrows;
+  if (M == 0 || N == 0) return GBS_OK;
+  Epilogue e;
+  make_epilogue(c, e, c->rowsum);
+  if (e.ra || e.rb) {
+    const Mat &reg = c->lhs.bipolar() ? c->rhs : c->lhs;
+    cudaError_t re = launch_rowsum(reg, c->rowsum, s);
+    if (re != cudaSuccess) return cuda_fail(re, "gbs_gemm: row-sum kernel");
+  }
+  GemmShape sh;
+  sh.A = c->lhs.planes;
+  sh.B = c->rhs.planes;
+  sh.C = c->res;
+  sh.M = M;
+  sh.N = N;
+  sh.wpr = c->lhs.wpr();
+  sh.a_plane = c->lhs.nrows_a * sh.wpr;
+  sh.b_plane = c->rhs.nrows_a * sh.wpr;
+  sh.wa = (int)c->lhs.nbits;
+  sh.wb = (int)c->rhs.nbits;
+  const int pipe = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
+  cudaError_t ke;
+  if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) ke = launch_gemm_bmma(sh, e, s);
+  else ke = launch_gemm_popc(sh, e, s);
+  if (ke != cudaSuccess) return cuda_fail(ke, "gbs_gemm: forward kernel");
+  return GBS_OK;
+}
+
+int gbs_get_result(gbs_ctx *c, int32_t *dst, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_get_result: ctx is NULL");
+  const uint64_t n = c->lhs.nrows * c->rhs.nrows;
+  if (n == 0) return GBS_OK;
+  if (!dst) return fail(GBS_EINVAL, "gbs_get_result: dst is NULL");
+  DeviceGuard g(c->device);
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(dst, c->res, n * 4, cudaMemcpyDefault, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_get_result: copy");
+  if (!is_device_ptr(dst)) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_get_result: stream sync");
+  }
+  return GBS_OK;
+}
+
+int gbs_get_planes(gbs_ctx *c, int side, uint64_t *dst, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_get_planes: ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_get_planes: bad side");
+  const Mat &m = side ? c->rhs : c->lhs;
+  if (m.words() == 0) return GBS_OK;
+  if (!dst) return fail(GBS_EINVAL, "gbs_get_planes: dst is NULL");
+  DeviceGuard g(c->device);
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(dst, m.planes, m.words() * 8, cudaMemcpyDefault, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_get_planes: copy");
+  if (!is_device_ptr(dst)) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_get_planes: stream sync");
+  }
+  return GBS_OK;
+}
+
+static int to_dst(gbs_ctx *c, int32_t *dst, uint64_t n, cudaStream_t s,
+                  cudaError_t (*fill)(const Mat &, int32_t *, cudaStream_t), const Mat &m, const char *who) {
+  if (n == 0) return GBS_OK;
+  if (!dst) return fail(GBS_EINVAL, std::string(who) + ": dst is NULL");
+  if (is_device_ptr(dst)) {
+    cudaError_t e = fill(m, dst, s);
+    return e == cudaSuccess ? GBS_OK : cuda_fail(e, who);
+  }
+  int32_t *tmp = nullptr;
+  if (dev_alloc((void **)&tmp, n * 4) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GBS_ENOMEM, std::string(who) + ": temporary allocation failed");
+  }
+  cudaError_t e = fill(m, tmp, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, n * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(tmp);
+  return e == cudaSuccess ? GBS_OK : cuda_fail(e, who);
+}
+
+int gbs_sum_rows(gbs_ctx *c, int side, int32_t *dst, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_sum_rows: ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_sum_rows: bad side");
+  DeviceGuard g(c->device);
+  const Mat &m = side ? c->rhs : c->lhs;
+  return to_dst(c, dst, m.nrows, as_stream(stream), launch_rowsum, m, "gbs_sum_rows");
+}
+
+int gbs_export(gbs_ctx *c, int side, int32_t *dst, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_export: ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_export: bad side");
+  DeviceGuard g(c->device);
+  const Mat &m = side ? c->rhs : c->lhs;
+  return to_dst(c, dst, m.nrows * m.ncols, as_stream(stream), launch_export, m, "gbs_export");
+}
+
+}  // extern "C"

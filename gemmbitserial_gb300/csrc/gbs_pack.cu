@@ -1,0 +1,206 @@
+// gbs_pack.cu -- packing of regular integer matrices into bit planes, and the
+// plane-reading helpers (row sums, export).
+//
+// Semantics follow BitSerialMatrix::importRegular<T> (gemmbitserial.hpp:213-245),
+// its quantize step (:170-186) and the uint8_t overload (:249-275): element
+// (r, c) of plane b is bit b of the element's code, where the code is
+//   * the raw byte for uint8 input (no quantisation),
+//   * 1 if x > 0 else 0 for bipolar matrices (1-bit signed),
+//   * the low byte of x otherwise (two's complement for signed matrices; the
+//     reference's "add 2^(w-1) twice" leaves the low w bits of x unchanged).
+// Rows >= nrows and columns >= ncols are zero in every plane.
+#include "gbs_internal.h"
+
+namespace gbs {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int64_t load_elem(const void *src, int dtype, uint64_t idx) {
+  switch (dtype) {
+    case GBS_I8: return ((const int8_t *)src)[idx];
+    case GBS_U8: return ((const uint8_t *)src)[idx];
+    case GBS_I16: return ((const int16_t *)src)[idx];
+    default: return ((const int32_t *)src)[idx];
+  }
+}
+
+__device__ __forceinline__ uint32_t code_of(int64_t x, int dtype, int bipolar) {
+  if (dtype == GBS_U8) return (uint32_t)(x & 0xff);
+  if (bipolar) return x > 0 ? 1u : 0u;
+  return (uint32_t)(x & 0xff);
+}
+
+// Bits b of the four bytes of x, gathered into a nibble (byte i -> bit i).
+// (x>>b)&0x01010101 leaves one bit per byte at positions 0, 8, 16, 24; the
+// multiply by 1 + 2^7 + 2^14 + 2^21 lands them, carry-free, at 21..24.
+__device__ __forceinline__ uint32_t nibble(uint32_t x, int b) {
+  return ((((x >> b) & 0x01010101u) * 0x00204081u) >> 21) & 0xfu;
+}
+
+// Row-major pack.  One warp covers 512 columns (8 words) of one padded row;
+// lane l owns columns [16l, 16l+16) of that span, i.e. a quarter of word l/4.
+__global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
+                                                     int nbits, uint64_t nrows, uint64_t ncols,
+                                                     uint64_t nrows_a, uint64_t wpr, int vec,
+                                                     uint64_t *__restrict__ planes) {
+  const uint64_t segs = (wpr + 7) / 8;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nrows_a * segs) return;  // warp-uniform
+  const uint64_t r = warp / segs, seg = warp % segs;
+  const uint64_t col0 = seg * 512 + (uint64_t)lane * 16;
+  uint32_t q[4] = {0u, 0u, 0u, 0u};  // 16 codes, 4 per word, byte j%4 of q[j/4]
+  if (r < nrows && col0 < ncols) {
+    const uint64_t base = r * ncols + col0;
+    if (vec) {  // 1-byte elements, 16-byte aligned rows
+      uint4 v = *reinterpret_cast<const uint4 *>((const uint8_t *)src + base);
+      q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w;
+      if (bipolar && dtype == GBS_I8) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) q[i] = __vcmpgts4(q[i], 0u) & 0x01010101u;
+      }
+    } else {
+#pragma unroll 4
+      for (int j = 0; j < 16; j++) {
+        if (col0 + j < ncols) q[j >> 2] |= code_of(load_elem(src, dtype, base + j), dtype, bipolar) << (8 * (j & 3));
+      }
+    }
+  }
+  const uint64_t w = seg * 8 + (lane >> 2);
+  const uint64_t plane_words = nrows_a * wpr;
+  for (int b = 0; b < nbits; b++) {
+    uint32_t m16 = nibble(q[0], b) | (nibble(q[1], b) << 4) | (nibble(q[2], b) << 8) | (nibble(q[3], b) << 12);
+    uint64_t v = (uint64_t)m16 << (16 * (lane & 3));
+    v |= __shfl_xor_sync(kFull, v, 1);
+    v |= __shfl_xor_sync(kFull, v, 2);
+    if ((lane & 3) == 0 && w < wpr) planes[b * plane_words + r * wpr + w] = v;
+  }
+}
+
+// Column-major pack (the reference's readColMajor: element (r, c) at c*nrows + r).
+// One warp covers 32 padded rows x 64 columns (one word per row and plane):
+// lane l reads column c0+l (then c0+32+l) down the 32 rows, and one ballot per
+// (row, plane) gathers 32 columns of that row.  Lane j keeps row j's word.
+__global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ src, int dtype, int bipolar,
+                                                     int nbits, uint64_t nrows, uint64_t ncols,
+                                                     uint64_t nrows_a, uint64_t wpr,
+                                                     uint64_t *__restrict__ planes) {
+  const uint64_t rgroups = nrows_a / 32;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= rgroups * wpr) return;  // warp-uniform
+  const uint64_t w = warp / rgroups, r0 = (warp % rgroups) * 32;
+  uint32_t lo[kMaxBits], hi[kMaxBits];
+#pragma unroll
+  for (int b = 0; b < kMaxBits; b++) lo[b] = hi[b] = 0u;
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const uint64_t c = w * 64 + half * 32 + lane;
+    uint32_t q[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};  // codes of rows r0..r0+31 of column c
+    if (c < ncols) {
+      for (int j = 0; j < 32; j++) {
+        uint64_t r = r0 + j;
+        if (r < nrows) q[j >> 2] |= code_of(load_elem(src, dtype, c * nrows + r), dtype, bipolar) << (8 * (j & 3));
+      }
+    }
+    for (int j = 0; j < 32; j++) {
+      uint32_t code = (q[j >> 2] >> (8 * (j & 3))) & 0xffu;
+#pragma unroll
+      for (int b = 0; b < kMaxBits; b++) {
+        if (b < nbits) {
+          uint32_t m = __ballot_sync(kFull, (code >> b) & 1u);
+          if (lane == j) { if (half) hi[b] = m; else lo[b] = m; }
+        }
+      }
+    }
+  }
+  const uint64_t plane_words = nrows_a * wpr;
+  const uint64_t r = r0 + lane;
+#pragma unroll
+  for (int b = 0; b < kMaxBits; b++)
+    if (b < nbits) planes[b * plane_words + r * wpr + w] = (uint64_t)lo[b] | ((uint64_t)hi[b] << 32);
+}
+
+// sumRows (arch-generic.hpp:6-37): one warp per row.  uint32 arithmetic
+// reproduces the reference's int32 wrap-around.
+__global__ void __launch_bounds__(256) rowsum_kernel(const uint64_t *__restrict__ planes, int nbits, int issigned,
+                                                     uint64_t nrows, uint64_t ncols, uint64_t nrows_a,
+                                                     uint64_t wpr, int32_t *__restrict__ dst) {
+  const uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= nrows) return;
+  const bool bip = nbits == 1 && issigned;
+  uint32_t acc = 0;
+  for (int b = 0; b < nbits; b++) {
+    const uint64_t *row = planes + (uint64_t)b * nrows_a * wpr + r * wpr;
+    uint32_t cnt = 0;
+    for (uint64_t w = lane; w < wpr; w += 32) cnt += __popcll(row[w]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+    cnt <<= b;
+    if (issigned && !bip && b == nbits - 1) cnt = 0u - cnt;
+    acc += cnt;
+  }
+  if (bip) acc = 2u * acc - (uint32_t)ncols;
+  if (lane == 0) dst[r] = (int32_t)acc;
+}
+
+// exportRegular (gemmbitserial.hpp:313-333): one thread per element.
+__global__ void __launch_bounds__(256) export_kernel(const uint64_t *__restrict__ planes, int nbits, int issigned,
+                                                     uint64_t nrows, uint64_t ncols, uint64_t nrows_a,
+                                                     uint64_t wpr, int32_t *__restrict__ dst) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows * ncols) return;
+  const uint64_t r = i / ncols, c = i % ncols;
+  const bool bip = nbits == 1 && issigned;
+  int32_t v = 0;
+  for (int b = 0; b < nbits; b++) {
+    uint64_t bit = (planes[(uint64_t)b * nrows_a * wpr + r * wpr + (c >> 6)] >> (c & 63)) & 1u;
+    if (bip) v = bit ? 1 : -1;
+    else if (bit) v += (issigned && b == nbits - 1) ? -(1 << b) : (1 << b);
+  }
+  dst[i] = v;
+}
+
+inline unsigned blocks_for(uint64_t threads, unsigned per_block) {
+  return (unsigned)((threads + per_block - 1) / per_block);
+}
+
+}  // namespace
+
+cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major, cudaStream_t s) {
+  if (m.nrows_a == 0 || m.wpr() == 0) return cudaSuccess;
+  const int bip = m.bipolar() ? 1 : 0;
+  if (!col_major) {
+    const size_t esz = dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1;
+    const int vec = (esz == 1 && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0) ? 1 : 0;
+    const uint64_t warps = m.nrows_a * ((m.wpr() + 7) / 8);
+    pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
+                                                            m.nrows_a, m.wpr(), vec, m.planes);
+  } else {
+    const uint64_t warps = (m.nrows_a / 32) * m.wpr();
+    pack_colmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
+                                                            m.nrows_a, m.wpr(), m.planes);
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rowsum(const Mat &m, int32_t *dst, cudaStream_t s) {
+  if (m.nrows == 0) return cudaSuccess;
+  rowsum_kernel<<<blocks_for(m.nrows * 32, 256), 256, 0, s>>>(m.planes, (int)m.nbits, m.issigned, m.nrows,
+                                                              m.ncols, m.nrows_a, m.wpr(), dst);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export(const Mat &m, int32_t *dst, cudaStream_t s) {
+  if (m.nrows * m.ncols == 0) return cudaSuccess;
+  export_kernel<<<blocks_for(m.nrows * m.ncols, 256), 256, 0, s>>>(m.planes, (int)m.nbits, m.issigned, m.nrows,
+                                                                   m.ncols, m.nrows_a, m.wpr(), dst);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace gbs

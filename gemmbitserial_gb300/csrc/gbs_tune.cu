@@ -1,0 +1,126 @@
+// gbs_tune.cu -- pipe peaks and the per-shape pipe choice.
+//
+// gbs_pipe_peaks measures, on the current device, the sustained rate of the
+// two pipes the forward GEMM can use, in AND+popcount bit operations per
+// second (one bit of one plane pair of one output):
+//   * POPC: a shared-memory-fed 4x4 register tile of popc(a & b) over 64-bit
+//     words, the inner loop of the CUDA-core kernel;
+//   * BMMA: back-to-back mma.sync.m16n8k256 b1 AND.popc with independent
+//     accumulators.
+// Both loops run on every SM (4 CTAs of 256 threads each) for ~10-20 ms.
+#include <cstdio>
+
+#include "gbs_internal.h"
+
+namespace gbs {
+namespace {
+
+__global__ void __launch_bounds__(256) peak_popc(const uint64_t *in, int *out, int iters) {
+  __shared__ uint64_t sa[64 * 16], sb[64 * 16];
+  for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) {
+    sa[i] = in[i & 1023];
+    sb[i] = in[(i * 7) & 1023];
+  }
+  __syncthreads();
+  uint32_t acc[4][4] = {};
+  const int tm = threadIdx.x & 15, tn = threadIdx.x >> 4;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll 4
+    for (int k = 0; k < 64; k++) {
+      uint64_t a[4], b[4];
+#pragma unroll
+      for (int m = 0; m < 4; m++) a[m] = sa[k * 16 + ((tm + m) & 15)];
+#pragma unroll
+      for (int n = 0; n < 4; n++) b[n] = sb[k * 16 + ((tn + n) & 15)];
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+#pragma unroll
+        for (int n = 0; n < 4; n++) acc[m][n] += __popcll(a[m] & b[n]);
+    }
+  }
+  uint32_t s = 0;
+  for (int m = 0; m < 4; m++)
+    for (int n = 0; n < 4; n++) s += acc[m][n];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = (int)s;
+}
+
+__global__ void __launch_bounds__(256) peak_bmma(const uint64_t *in64, int *out, int iters) {
+  const uint32_t *in = reinterpret_cast<const uint32_t *>(in64);
+  const int t = threadIdx.x;
+  uint32_t a0 = in[t & 127], a1 = in[(t + 1) & 127], a2 = in[(t + 2) & 127], a3 = in[(t + 3) & 127];
+  uint32_t b0 = in[(t + 4) & 127], b1 = in[(t + 5) & 127];
+  int c[4][4] = {};
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      asm volatile(
+          "mma.sync.aligned.m16n8k256.row.col.s32.b1.b1.s32.and.popc {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+          "{%0,%1,%2,%3};"
+          : "+r"(c[j][0]), "+r"(c[j][1]), "+r"(c[j][2]), "+r"(c[j][3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  int s = 0;
+  for (int j = 0; j < 4; j++) s += c[j][0] + c[j][1] + c[j][2] + c[j][3];
+  out[blockIdx.x * blockDim.x + t] = s;
+}
+
+}  // namespace
+
+int choose_pipe(const gbs_ctx *) {
+  // On GB300 the CUDA-core pipe sustains about twice the b1 tensor pipe's
+  // AND+popcount rate (gbs_pipe_peaks), for every shape class.
+  return GBS_PIPE_POPC;
+}
+
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" int gbs_pipe_peaks(double *popc_bitops, double *bmma_bitops) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "gbs_pipe_peaks: no device");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  uint64_t *in = nullptr;
+  int *out = nullptr;
+  const int blocks = sms * 4, threads = 256;
+  if (dev_alloc((void **)&in, 1024 * 8) != cudaSuccess || dev_alloc((void **)&out, blocks * threads * 4) != cudaSuccess) {
+    cudaGetLastError();
+    if (in) cudaFree(in);
+    return fail(GBS_ENOMEM, "gbs_pipe_peaks: allocation failed");
+  }
+  uint64_t h[1024];
+  for (int i = 0; i < 1024; i++) h[i] = 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
+  cudaMemcpy(in, h, sizeof(h), cudaMemcpyHostToDevice);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto timed = [&](auto launch) {
+    launch(4);
+    cudaDeviceSynchronize();
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+      cudaEventRecord(e0);
+      launch(0);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) best = ms;
+    }
+    return (double)best * 1e-3;
+  };
+  const int it_popc = 48, it_bmma = 2048;
+  double tp = timed([&](int small) { peak_popc<<<blocks, threads>>>(in, out, small ? small : it_popc); });
+  double tb = timed([&](int small) { peak_bmma<<<blocks, threads>>>(in, out, small ? small : it_bmma); });
+  count_launch(8);
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(in);
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_pipe_peaks");
+  const double warps = (double)blocks * threads / 32.0;
+  if (popc_bitops) *popc_bitops = warps * 32.0 * it_popc * 64.0 * 16.0 * 64.0 / tp;
+  if (bmma_bitops) *bmma_bitops = warps * it_bmma * 4.0 * 16.0 * 8.0 * 256.0 / tb;
+  return GBS_OK;
+}

@@ -1,0 +1,164 @@
+/*
+ * gbs.h -- C ABI of the GB300 bit-serial GEMM library (libgbs.so).
+ *
+ * This is the drop-in boundary for maltanar/gemmbitserial's hot path
+ *   allocGEMMContext -> lhs/rhs.importRegular -> gemmBitSerial -> ctx.res
+ *   -> deallocGEMMContext
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (GBS_OK on success).  On failure gbs_last_error() returns a message for the
+ * calling thread.  Device work is ordered on the caller's CUDA stream, passed
+ * as an opaque handle (a cudaStream_t; NULL selects the legacy default
+ * stream).  The C++ header gemmbitserial.hpp in this directory rebuilds the
+ * reference's class API on top of these calls.
+ *
+ * Matrix storage on the device keeps the reference's bit-serial layout
+ * (gemmbitserial.hpp:50): 64-bit words, [nbits][nrows_a][ncols_a/64], column c
+ * of row r in plane b at word c>>6, bit c&63, all padding zero.  The device
+ * pads rows to a multiple of 128 and columns to a multiple of 256 (the
+ * reference pads columns to 64, or to 256 for matrix-vector contexts, and
+ * rows to its cache block); results never depend on padding.
+ */
+#ifndef GBS_H_
+#define GBS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GBS_API __attribute__((visibility("default")))
+#else
+#define GBS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum {
+  GBS_OK = 0,
+  GBS_EINVAL = 1,      /* invalid argument (shape, width, null pointer, ...) */
+  GBS_ENOMEM = 2,      /* device or pinned-host allocation failed */
+  GBS_ECUDA = 3,       /* a CUDA runtime call failed */
+  GBS_ESTATE = 4,      /* call out of order (e.g. gemm before both imports) */
+  GBS_ETIMEOUT = 5,    /* a bounded device wait gave up */
+  GBS_EUNSUPPORTED = 6 /* valid request this build does not implement */
+};
+
+/* Element types accepted by gbs_import.  GBS_I8/I16/I32 follow the
+ * reference's importRegular<T> (gemmbitserial.hpp:213): bipolar matrices map
+ * x>0 to +1 and everything else to -1, other matrices keep the low nbits bits
+ * of x (two's complement).  GBS_U8 follows the reference's non-template
+ * uint8_t overload (gemmbitserial.hpp:249): raw low bits for every encoding. */
+enum { GBS_I8 = 0, GBS_U8 = 1, GBS_I16 = 2, GBS_I32 = 3 };
+
+enum { GBS_LHS = 0, GBS_RHS = 1 };
+
+/* Compute pipe of the forward GEMM. */
+enum {
+  GBS_PIPE_AUTO = 0, /* per-shape choice (tuner store, else built-in rule) */
+  GBS_PIPE_POPC = 1, /* CUDA cores: LOP3 AND/XOR + POPC */
+  GBS_PIPE_BMMA = 2  /* tensor pipe: mma.sync b1 AND/XOR + popc */
+};
+
+typedef struct gbs_ctx gbs_ctx; /* opaque; copies of the handle alias one context */
+
+typedef struct {
+  uint64_t nbits, nrows, ncols, nrows_a, ncols_a;
+  int issigned;
+  int isbipolar;
+  uint64_t *data; /* DEVICE pointer to the planes */
+} gbs_matrix_info;
+
+typedef struct {
+  gbs_matrix_info lhs, rhs;
+  uint64_t lhsBlock, rhsBlock; /* device tile rows (lhs, rhs) */
+  int32_t *res;                /* DEVICE pointer, rhs.nrows x lhs.nrows, transposed layout */
+  int pipe;                    /* pipe the next gbs_gemm will use */
+} gbs_ctx_info;
+
+/* Replaces allocGEMMContext / allocGEMMContext_generic (arch-generic.hpp:78-100,
+ * gemmbitserial.hpp:415-452, macro gemmbitserial.hpp:477).  lhsRows = M,
+ * depth = K, rhsRows = N; bits in [1, 8]; a 1-bit signed operand is bipolar
+ * {-1,+1} (gemmbitserial.hpp:74-76).  Allocates the planes and the result on
+ * the current CUDA device.  M, N or K may be 0 (empty result). */
+GBS_API int gbs_ctx_alloc(uint64_t lhsRows, uint64_t depth, uint64_t rhsRows, uint64_t lhsBits,
+                  uint64_t rhsBits, int lhsSigned, int rhsSigned, gbs_ctx **out);
+
+/* Alias of gbs_ctx_alloc under the name the reference README uses
+ * (README.md:15, "allocateGEMMContext"). */
+GBS_API int gbs_ctx_allocate(uint64_t lhsRows, uint64_t depth, uint64_t rhsRows, uint64_t lhsBits,
+                     uint64_t rhsBits, int lhsSigned, int rhsSigned, gbs_ctx **out);
+
+/* Replaces deallocGEMMContext (gemmbitserial.hpp:454-458).  Synchronises the
+ * device, then frees every buffer of the context.  NULL is a no-op. */
+GBS_API int gbs_ctx_free(gbs_ctx *ctx);
+
+/* Shapes, padding and device pointers of a context (the public fields of
+ * GEMMContext / BitSerialMatrix, gemmbitserial.hpp:44-50, 379-383). */
+GBS_API int gbs_ctx_get_info(const gbs_ctx *ctx, gbs_ctx_info *info);
+
+/* Replaces BitSerialMatrix::importRegular<T> (gemmbitserial.hpp:213-245) and
+ * its uint8_t overload (:249-275) for ctx.lhs (side 0, M x K) or ctx.rhs
+ * (side 1, N x K, i.e. B transposed).  src is row-major [rows][K], or
+ * [K][rows] when col_major (the reference's readColMajor).  src may be host
+ * memory (pageable or pinned) or device memory; host data is copied to the
+ * device first.  The packing runs on `stream`; with host src the call returns
+ * once src may be reused. */
+GBS_API int gbs_import(gbs_ctx *ctx, int side, const void *src, int dtype, int col_major, void *stream);
+
+/* Replaces gemmBitSerial / gemmBitSerial_generic (arch-generic.hpp:331-345,
+ * macro gemmbitserial.hpp:476): res = lhs * rhs^T in the transposed layout
+ * res[n*M + m], bit-exact with the reference (int32 with wrap-around).
+ * Asynchronous on `stream`. */
+GBS_API int gbs_gemm(gbs_ctx *ctx, void *stream);
+
+/* Copies the result (ctx.res in the reference, gemmbitserial.hpp:383) to dst,
+ * host or device memory of M*N int32.  With host dst the call returns after
+ * the copy has completed. */
+GBS_API int gbs_get_result(gbs_ctx *ctx, int32_t *dst, void *stream);
+
+/* Replaces sumRows / sumRows_generic (arch-generic.hpp:6-37, macro
+ * gemmbitserial.hpp:478) for one side of the context: dst[r] = sum of the
+ * values of row r.  dst is host or device memory of nrows int32. */
+GBS_API int gbs_sum_rows(gbs_ctx *ctx, int side, int32_t *dst, void *stream);
+
+/* Replaces BitSerialMatrix::exportRegular<int32_t> (gemmbitserial.hpp:313-333)
+ * for one side: dst[r*ncols + c] = value of element (r, c).  dst is host or
+ * device memory of nrows*ncols int32. */
+GBS_API int gbs_export(gbs_ctx *ctx, int side, int32_t *dst, void *stream);
+
+/* Copies the packed planes of one side (BitSerialMatrix::data,
+ * gemmbitserial.hpp:50) to dst, host or device memory of
+ * nbits * nrows_a * ncols_a/64 uint64 words.  With host dst the call returns
+ * after the copy has completed. */
+GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
+
+/* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
+GBS_API int gbs_set_pipe(gbs_ctx *ctx, int pipe);
+
+/* Measures the sustained AND+popcount rate (bit operations per second: one
+ * bit of one plane pair of one output) of the CUDA-core pipe and of the b1
+ * tensor pipe on the current device (~50 ms).  Either pointer may be NULL.
+ * No reference counterpart: the reference has a single CPU pipe. */
+GBS_API int gbs_pipe_peaks(double *popc_bitops, double *bmma_bitops);
+
+/* Message describing the last failure on the calling thread ("" if none). */
+GBS_API const char *gbs_last_error(void);
+
+/* Library version string. */
+GBS_API const char *gbs_version(void);
+
+/* ---- test hooks (host-side fault injection; no device faults) ---------- */
+
+/* Makes the n-th next allocation made by the library fail (n >= 1); 0 disarms. */
+GBS_API void gbs_debug_fail_alloc_after(int n);
+
+/* Number of kernel launches the library has issued since load (all entry points). */
+GBS_API uint64_t gbs_debug_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBS_H_ */
