@@ -45,8 +45,8 @@ DEFAULT_WORKLOAD = "gemm_2048x4096x2048_u3s2"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default=DEFAULT_WORKLOAD)
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU baseline sample")
@@ -142,22 +142,30 @@ def run_reference(args):
 # ---------------------------------------------------------------- GPU side
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons of this process's GPU, sampled every 100 ms while running."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
+        self.index = str(index)
+        try:
+            import torch
+            u = getattr(torch.cuda.get_device_properties(index), "uuid", None)
+            if u is not None:
+                self.index = "GPU-" + str(u)
+        except Exception:
+            pass
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.p = None
 
     def __enter__(self):
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)  # let the sampler start before the measured work
         except OSError:
             self.p = None
         return self
@@ -177,9 +185,10 @@ class ClockSampler:
         sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "window": "warm-up and timed loops of both the resident and the end-to-end measurement"}
 
 
 def read_traffic(kernel, workload):
@@ -225,13 +234,14 @@ def run_ours(args):
     stream.synchronize()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clk = ClockSampler(local).__enter__()
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.zero_()
             _capi.check(lib.gbs_gemm(ctx._h, sh))
     barrier()
     launches0 = lib.gbs_debug_launch_count()
-    with ClockSampler(local) as clk:
+    if True:
         barrier()
         t_wall = time.perf_counter()
         with torch.cuda.stream(stream):
@@ -277,6 +287,7 @@ def run_ours(args):
         e2e_step()
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
+    clk.__exit__()
     e2e_ok = hashlib.sha256(hR.numpy().tobytes()).hexdigest() == want
     deallocGEMMContext(ctx2)
     if world > 1:

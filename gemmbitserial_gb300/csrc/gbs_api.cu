@@ -158,7 +158,7 @@ int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, 
   if (e == cudaSuccess) { what = "lhs planes"; e = dev_alloc((void **)&c->lhs.planes, c->lhs.words() * 8); }
   if (e == cudaSuccess) { what = "rhs planes"; e = dev_alloc((void **)&c->rhs.planes, c->rhs.words() * 8); }
   if (e == cudaSuccess) { what = "result"; e = dev_alloc((void **)&c->res, M * N * 4); }
-  if (e == cudaSuccess) { what = "row sums"; e = dev_alloc((void **)&c->rowsum, (M > N ? M : N) * 4); }
+  if (e == cudaSuccess) { what = "row sums"; e = dev_alloc((void **)&c->rowsum, (M + N) * 4); }
   if (e != cudaSuccess) {
     cudaGetLastError();
     free_ctx_buffers(c);
@@ -291,8 +291,22 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.wb = (int)c->rhs.nbits;
   const int pipe = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
   cudaError_t ke;
-  if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) ke = launch_gemm_bmma(sh, e, s);
-  else ke = launch_gemm_popc(sh, e, s);
+  if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
+    if (e.use_xor) {
+      // ncols - 2*popc(a^b) = 4*popc(a&b) - rsA - rsB - ncols, rs = bipolar row sums (2*popc - ncols)
+      e.use_xor = 0;
+      e.alpha[0][0] = 4;
+      e.c0 = 0u - (uint32_t)c->lhs.ncols;
+      e.ra = c->rowsum;
+      e.rb = c->rowsum + M;
+      cudaError_t re = launch_rowsum(c->lhs, c->rowsum, s);
+      if (re == cudaSuccess) re = launch_rowsum(c->rhs, c->rowsum + M, s);
+      if (re != cudaSuccess) return cuda_fail(re, "gbs_gemm: row-sum kernel");
+    }
+    ke = launch_gemm_bmma(sh, e, s);
+  } else {
+    ke = launch_gemm_popc(sh, e, s);
+  }
   if (ke != cudaSuccess) return cuda_fail(ke, "gbs_gemm: forward kernel");
   return GBS_OK;
 }

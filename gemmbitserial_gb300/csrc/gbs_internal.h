@@ -49,7 +49,7 @@ struct gbs_ctx {
   gbs::Mat lhs, rhs;
   uint64_t lhsBlock = 0, rhsBlock = 0;
   int32_t *res = nullptr;     // [N][M]
-  int32_t *rowsum = nullptr;  // scratch: row sums of the regular operand, max(M, N) entries
+  int32_t *rowsum = nullptr;  // scratch: row sums, lhs rows at [0, M), rhs rows at [M, M+N)
   void *stage = nullptr;      // device staging for host-side imports
   size_t stage_bytes = 0;
   int device = 0;

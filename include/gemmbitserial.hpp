@@ -1,0 +1,160 @@
+// gemmbitserial.hpp -- drop-in C++ API of maltanar/gemmbitserial over libgbs.
+//
+// Source-compatible with the reference's hot path
+//   GEMMContext ctx = allocGEMMContext(M, K, N, lhsBits, rhsBits, lhsSigned, rhsSigned);
+//   ctx.lhs.importRegular(A);   ctx.rhs.importRegular(BT);
+//   gemmBitSerial(ctx);         // ctx.res holds the N x M (transposed) int32 result
+//   deallocGEMMContext(ctx);
+// plus sumRows, BitSerialMatrix::alloc/dealloc and exportRegular.  Link with
+// -lgbs.  All compute runs on the current CUDA device; the packed planes live
+// in device memory (BitSerialMatrix::data is a DEVICE pointer), ctx.res is a
+// host array filled when gemmBitSerial returns.
+//
+// Like the reference, GEMMContext and BitSerialMatrix are plain values:
+// copies alias the same context (gemmbitserial.hpp:454-458 of the reference
+// frees through any copy).  Errors throw std::runtime_error with the
+// library's message, where the reference would assert.
+#pragma once
+
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+
+#include "gbs.h"
+
+namespace gemmbitserial {
+
+namespace detail {
+inline void check(int rc) {
+  if (rc != GBS_OK) throw std::runtime_error(std::string("gemmbitserial: ") + gbs_last_error());
+}
+template <typename T> struct elem;
+template <> struct elem<int8_t> { static const int code = GBS_I8; };
+template <> struct elem<int16_t> { static const int code = GBS_I16; };
+template <> struct elem<int32_t> { static const int code = GBS_I32; };
+}  // namespace detail
+
+class BitSerialMatrix {
+ public:
+  bool issigned = false;
+  uint64_t nbits = 0, nrows = 0, ncols = 0, nrows_a = 0, ncols_a = 0;
+  uint64_t *data = nullptr;  // device planes [nbits][nrows_a][ncols_a/64]
+
+  gbs_ctx *ctx_ = nullptr;  // owning context (shared by copies)
+  int side_ = GBS_LHS;
+
+  // BitSerialMatrix::alloc (reference gemmbitserial.hpp:24-35).  The device
+  // chooses its own padding, so rowalign/colalign are accepted and ignored.
+  static BitSerialMatrix alloc(uint64_t nbits, uint64_t nrows, uint64_t ncols, bool issigned,
+                               uint64_t rowalign = 1, uint64_t colalign = 64) {
+    (void)rowalign;
+    (void)colalign;
+    gbs_ctx *c = nullptr;
+    detail::check(gbs_ctx_alloc(nrows, ncols, 0, nbits, 1, issigned ? 1 : 0, 0, &c));
+    return from_ctx(c, GBS_LHS);
+  }
+
+  // BitSerialMatrix::dealloc (reference gemmbitserial.hpp:38-40) for matrices made by alloc().
+  static void dealloc(BitSerialMatrix bsm) { detail::check(gbs_ctx_free(bsm.ctx_)); }
+
+  static BitSerialMatrix from_ctx(gbs_ctx *c, int side) {
+    gbs_ctx_info info;
+    detail::check(gbs_ctx_get_info(c, &info));
+    const gbs_matrix_info &m = side ? info.rhs : info.lhs;
+    BitSerialMatrix b;
+    b.issigned = m.issigned != 0;
+    b.nbits = m.nbits;
+    b.nrows = m.nrows;
+    b.ncols = m.ncols;
+    b.nrows_a = m.nrows_a;
+    b.ncols_a = m.ncols_a;
+    b.data = m.data;
+    b.ctx_ = c;
+    b.side_ = side;
+    return b;
+  }
+
+  bool isBipolar() const { return nbits == 1 && issigned; }
+  uint64_t wordsPerRow() const { return ncols_a / 64; }
+  uint64_t wordsPerBitplane() const { return nrows_a * wordsPerRow(); }
+
+  // importRegular<T> (reference gemmbitserial.hpp:213): int8/int16/int32,
+  // host or device memory, row-major or (readColMajor) column-major.
+  template <typename T>
+  void importRegular(T *matrix, bool readColMajor = false) {
+    detail::check(gbs_import(ctx_, side_, matrix, detail::elem<T>::code, readColMajor ? 1 : 0, nullptr));
+  }
+  // The uint8_t overload (reference gemmbitserial.hpp:249): raw low bits.
+  void importRegular(uint8_t *matrix, bool readColMajor = false) {
+    detail::check(gbs_import(ctx_, side_, matrix, GBS_U8, readColMajor ? 1 : 0, nullptr));
+  }
+
+  // exportRegular<T> (reference gemmbitserial.hpp:313-333) into host memory.
+  template <typename T>
+  void exportRegular(T *matrix) {
+    const uint64_t n = nrows * ncols;
+    if (n == 0) return;
+    int32_t *tmp = new int32_t[n];
+    int rc = gbs_export(ctx_, side_, tmp, nullptr);
+    if (rc == GBS_OK)
+      for (uint64_t i = 0; i < n; i++) matrix[i] = (T)tmp[i];
+    delete[] tmp;
+    detail::check(rc);
+  }
+};
+
+class GEMMContext {
+ public:
+  BitSerialMatrix lhs, rhs;
+  uint64_t lhsBlock = 0, rhsBlock = 0;
+  int32_t *res = nullptr;  // host, rhs.nrows x lhs.nrows (transposed result)
+  gbs_ctx *handle = nullptr;
+
+  bool isBipolarTimesRegular() const { return lhs.isBipolar() != rhs.isBipolar(); }
+  bool isBipolarTimesBipolar() const { return lhs.isBipolar() && rhs.isBipolar(); }
+  bool isMatrixVector() const { return rhs.nrows == 1; }
+};
+
+// allocGEMMContext (reference arch-generic.hpp:78-100, gemmbitserial.hpp:415-452).
+inline GEMMContext allocGEMMContext(uint64_t lhsRows, uint64_t depth, uint64_t rhsRows, uint64_t lhsBits,
+                                    uint64_t rhsBits, bool lhsSigned, bool rhsSigned) {
+  gbs_ctx *c = nullptr;
+  detail::check(gbs_ctx_alloc(lhsRows, depth, rhsRows, lhsBits, rhsBits, lhsSigned ? 1 : 0, rhsSigned ? 1 : 0, &c));
+  GEMMContext g;
+  g.handle = c;
+  g.lhs = BitSerialMatrix::from_ctx(c, GBS_LHS);
+  g.rhs = BitSerialMatrix::from_ctx(c, GBS_RHS);
+  gbs_ctx_info info;
+  detail::check(gbs_ctx_get_info(c, &info));
+  g.lhsBlock = info.lhsBlock;
+  g.rhsBlock = info.rhsBlock;
+  g.res = new int32_t[lhsRows * rhsRows + 1];
+  return g;
+}
+
+// The name the reference README uses (README.md:15).
+inline GEMMContext allocateGEMMContext(uint64_t lhsRows, uint64_t depth, uint64_t rhsRows, uint64_t lhsBits,
+                                       uint64_t rhsBits, bool lhsSigned, bool rhsSigned) {
+  return allocGEMMContext(lhsRows, depth, rhsRows, lhsBits, rhsBits, lhsSigned, rhsSigned);
+}
+
+// gemmBitSerial (reference arch-generic.hpp:331-345): runs on the GPU and
+// leaves the result in ctx.res when it returns.
+inline void gemmBitSerial(GEMMContext ctx) {
+  detail::check(gbs_gemm(ctx.handle, nullptr));
+  detail::check(gbs_get_result(ctx.handle, ctx.res, nullptr));
+}
+
+// deallocGEMMContext (reference gemmbitserial.hpp:454-458).
+inline void deallocGEMMContext(GEMMContext ctx) {
+  delete[] ctx.res;
+  detail::check(gbs_ctx_free(ctx.handle));
+}
+
+// sumRows (reference arch-generic.hpp:6-37, macro gemmbitserial.hpp:478).
+inline void sumRows(BitSerialMatrix m, int32_t *row_sums) {
+  detail::check(gbs_sum_rows(m.ctx_, m.side_, row_sums, nullptr));
+}
+
+}  // namespace gemmbitserial

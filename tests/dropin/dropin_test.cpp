@@ -1,0 +1,174 @@
+// Drop-in check: code written against the reference's C++ API, compiled
+// against include/gemmbitserial.hpp and linked with libgbs.so.  Groups follow
+// the reference's test/test.cpp (conversions, row sums, matrix-matrix and
+// matrix-vector, bipolar x regular both ways, bipolar x bipolar), compared in
+// full against a naive integer GEMM (test/testhelpers.hpp:34-45).  Inputs come
+// from a fixed-seed generator, so runs are reproducible.  Exit status is the
+// number of failed groups.
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "gemmbitserial.hpp"
+
+using namespace gemmbitserial;
+
+static uint64_t rng_state = 0x6762730000ull;
+static uint64_t next_u64() {
+  uint64_t z = (rng_state += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+template <typename T>
+static void fill(std::vector<T> &v, int bits, bool sgn) {
+  for (auto &x : v) {
+    if (bits == 1 && sgn) x = (next_u64() & 1) ? 1 : -1;
+    else if (sgn) x = (T)((int)(next_u64() % (1u << bits)) - (1 << (bits - 1)));
+    else x = (T)(next_u64() % (1u << bits));
+  }
+}
+template <typename L, typename R>
+static void naive(const std::vector<L> &a, const std::vector<R> &b, std::vector<int32_t> &c, int M, int K, int N) {
+  for (int n = 0; n < N; n++)
+    for (int m = 0; m < M; m++) {
+      int32_t acc = 0;
+      for (int k = 0; k < K; k++) acc += (int32_t)a[m * K + k] * (int32_t)b[n * K + k];
+      c[n * M + m] = acc;
+    }
+}
+
+static int report(const char *name, int ok, int total) {
+  printf("%s: %d/%d OK\n", name, ok, total);
+  return ok == total ? 0 : 1;
+}
+
+int main() {
+  const int dims[] = {3, 5, 7, 16, 17, 18, 30, 31, 32, 100, 177, 256};
+  int failed = 0;
+  {  // import -> export round trip, all d*d elements
+    int ok = 0, total = 0;
+    for (int b : {1, 2, 3, 7})
+      for (int d : {4, 16, 17, 32, 77, 100, 1023})
+        for (int s : {1, 0}) {
+          std::vector<int8_t> x(d * d), y(d * d);
+          fill(x, b, s);
+          BitSerialMatrix m = BitSerialMatrix::alloc(b, d, d, s);
+          m.importRegular(x.data());
+          m.exportRegular(y.data());
+          BitSerialMatrix::dealloc(m);
+          ok += memcmp(x.data(), y.data(), d * d) == 0;
+          total++;
+        }
+    failed += report("conversions", ok, total);
+  }
+  {  // sumRows on a copy of ctx.lhs, all d sums
+    int ok = 0, total = 0;
+    for (int b : {1, 2, 3, 4})
+      for (int d : {4, 16, 17, 32, 77, 100, 1023})
+        for (int s : {1, 0}) {
+          std::vector<int8_t> x(d * d);
+          fill(x, b, s);
+          std::vector<int32_t> got(d), want(d, 0);
+          GEMMContext ctx = allocGEMMContext(d, d, 1, b, 1, s, false);
+          BitSerialMatrix bsm = ctx.lhs;
+          bsm.importRegular(x.data());
+          sumRows(bsm, got.data());
+          deallocGEMMContext(ctx);
+          for (int r = 0; r < d; r++)
+            for (int c = 0; c < d; c++) want[r] += x[r * d + c];
+          ok += got == want;
+          total++;
+        }
+    failed += report("row sums", ok, total);
+  }
+  {  // unsigned matrix x matrix (d x 2d x 3d) and matrix x vector, uint8 overload
+    int ok = 0, total = 0;
+    for (int b : {2, 3, 4})
+      for (int d : dims)
+        for (int mv : {0, 1}) {
+          int M = d, K = 2 * d, N = mv ? 1 : 3 * d;
+          std::vector<uint8_t> a(M * K), bt(N * K);
+          fill(a, b, false);
+          fill(bt, b, false);
+          std::vector<int32_t> want(M * N);
+          naive(a, bt, want, M, K, N);
+          GEMMContext ctx = allocGEMMContext(M, K, N, b, b, false, false);
+          ctx.lhs.importRegular(a.data());
+          ctx.rhs.importRegular(bt.data());
+          gemmBitSerial(ctx);
+          ok += memcmp(ctx.res, want.data(), M * N * 4) == 0;
+          total++;
+          deallocGEMMContext(ctx);
+        }
+    failed += report("matrix-matrix / matrix-vector", ok, total);
+  }
+  {  // bipolar x regular, lhs/rhs swapped and not, signed and unsigned
+    int ok = 0, total = 0;
+    for (int sw : {0, 1})
+      for (int b : {2, 3, 4})
+        for (int d : dims)
+          for (int s : {1, 0}) {
+            std::vector<int8_t> bip(d * d), reg(d * d);
+            fill(bip, 1, true);
+            fill(reg, b, s);
+            std::vector<int32_t> want(d * d);
+            GEMMContext ctx;
+            if (sw) {
+              ctx = allocGEMMContext(d, d, d, b, 1, s, true);
+              ctx.lhs.importRegular(reg.data());
+              ctx.rhs.importRegular(bip.data());
+              naive(reg, bip, want, d, d, d);
+            } else {
+              ctx = allocGEMMContext(d, d, d, 1, b, true, s);
+              ctx.lhs.importRegular(bip.data());
+              ctx.rhs.importRegular(reg.data());
+              naive(bip, reg, want, d, d, d);
+            }
+            gemmBitSerial(ctx);
+            ok += memcmp(ctx.res, want.data(), d * d * 4) == 0;
+            total++;
+            deallocGEMMContext(ctx);
+          }
+    failed += report("bipolar x regular", ok, total);
+  }
+  {  // bipolar x bipolar, GEMM and GEMV
+    int ok = 0, total = 0;
+    for (int d : dims)
+      for (int mv : {0, 1}) {
+        int N = mv ? 1 : d;
+        std::vector<int8_t> a(d * d), bt(N * d);
+        fill(a, 1, true);
+        fill(bt, 1, true);
+        std::vector<int32_t> want(d * N);
+        naive(a, bt, want, d, d, N);
+        GEMMContext ctx = allocGEMMContext(d, d, N, 1, 1, true, true);
+        ctx.lhs.importRegular(a.data());
+        ctx.rhs.importRegular(bt.data());
+        gemmBitSerial(ctx);
+        ok += memcmp(ctx.res, want.data(), d * N * 4) == 0;
+        total++;
+        deallocGEMMContext(ctx);
+      }
+    failed += report("bipolar x bipolar", ok, total);
+  }
+  {  // by-value copies alias one context (as the reference's benchmark.cpp:205 relies on)
+    std::vector<int8_t> a(40 * 70), bt(30 * 70);
+    fill(a, 3, true);
+    fill(bt, 2, false);
+    std::vector<int32_t> want(40 * 30);
+    naive(a, bt, want, 40, 70, 30);
+    std::vector<GEMMContext> v;
+    v.push_back(allocGEMMContext(40, 70, 30, 3, 2, true, false));
+    GEMMContext copy = v[0];
+    copy.lhs.importRegular(a.data());
+    v[0].rhs.importRegular(bt.data());
+    gemmBitSerial(v[0]);
+    failed += report("aliasing copies", memcmp(v[0].res, want.data(), want.size() * 4) == 0, 1);
+    deallocGEMMContext(copy);
+  }
+  printf(failed ? "Some tests failed\n" : "All tests completed successfully\n");
+  return failed;
+}
