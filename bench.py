@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--workload", default=DEFAULT_WORKLOAD)
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-problem measurement")
     return p.parse_args()
 
 
@@ -200,6 +201,71 @@ def read_traffic(kernel, workload):
     return float(m.group(1)) if m else None
 
 
+def measure_grouped(lib, dev, stream, reps=5, warmup=2):
+    """512-problem mix: plain per-problem path vs one persistent grouped launch (and its CUDA graph)."""
+    import torch
+    from gemmbitserial_gb300 import _capi, datagen
+    from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext
+    from gemmbitserial_gb300.grouped import Group
+    mix = datagen.grouped_mix()
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4321)
+    ops = [(datagen.torch_operand(gen, M, K, wA, eA, dev), datagen.torch_operand(gen, N, K, wB, eB, dev))
+           for (M, K, N, wA, eA, wB, eB) in mix]
+    ctxs = [allocGEMMContext(M, K, N, wA, wB, eA != "u", eB != "u") for (M, K, N, wA, eA, wB, eB) in mix]
+    sh = C.c_void_p(stream.cuda_stream)
+    L = (C.c_void_p * len(ops))(*[a.data_ptr() for a, _ in ops])
+    R = (C.c_void_p * len(ops))(*[b.data_ptr() for _, b in ops])
+
+    def plain_gemm():
+        for c in ctxs:
+            _capi.check(lib.gbs_gemm(c._h, sh))
+
+    def plain_full():
+        for c, (a, b) in zip(ctxs, ops):
+            _capi.check(lib.gbs_import(c._h, 0, C.c_void_p(a.data_ptr()), _capi.GBS_I8, 0, sh))
+            _capi.check(lib.gbs_import(c._h, 1, C.c_void_p(b.data_ptr()), _capi.GBS_I8, 0, sh))
+            _capi.check(lib.gbs_gemm(c._h, sh))
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    with torch.cuda.stream(stream):
+        t_plain_full = timed(plain_full)
+        t_plain = timed(plain_gemm)
+        ref = [c.res.copy() for c in ctxs[:: 37]]
+        g = Group(ctxs)
+        t_group = timed(lambda: _capi.check(lib.gbs_group_gemm(g._h, sh)))
+        _capi.check(lib.gbs_group_capture(g._h, L, R, None, sh))
+        t_graph = timed(lambda: _capi.check(lib.gbs_group_replay(g._h, sh)))
+    ok = lib.gbs_group_status(g._h, sh) == 0 and all(
+        np.array_equal(r, c.res) for r, c in zip(ref, ctxs[:: 37]))
+    stats = g.stats()
+    g.free()
+    for c in ctxs:
+        deallocGEMMContext(c)
+    gops_total = sum(2.0 * M * K * N for (M, K, N, *_r) in mix)
+    binops = sum(2.0 * M * N * ((K + 63) // 64 * 64) * wA * wB for (M, K, N, wA, _a, wB, _b) in mix)
+    return {"problems": len(mix), "plain_gemm_ms": round(t_plain, 4), "grouped_gemm_ms": round(t_group, 4),
+            "speedup_gemm": round(t_plain / t_group, 3),
+            "plain_pack_gemm_ms": round(t_plain_full, 4), "graph_pack_gemm_ms": round(t_graph, 4),
+            "speedup_pack_gemm": round(t_plain_full / t_graph, 3),
+            "grouped_gops": round(gops_total / (t_group * 1e-3) / 1e9, 1),
+            "grouped_tbinops": round(binops / (t_group * 1e-3) / 1e12, 2),
+            "tiles": stats["tiles"], "grid": stats["grid"], "smem_bytes": stats["smem_bytes"],
+            "parity": "grouped == plain (sampled 14 problems)" if ok else "MISMATCH",
+            "mix": "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -309,6 +375,8 @@ def run_ours(args):
     traffic = read_traffic(kernel, args.workload)
     clocks = clk.summary()
 
+    grouped = None if args.no_grouped else measure_grouped(lib, dev, stream)
+
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         threads = os.cpu_count() or 1
@@ -330,6 +398,7 @@ def run_ours(args):
                          "peak_source": "measured in-process (gbs_pipe_peaks: CUDA-core AND+POPC loop)",
                          "bmma_peak": round(2.0 * bmma.value / 1e12, 3),
                          "traffic": traffic, "algorithmic_bytes": int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)},
+            "grouped": grouped,
             "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
             "wall_s_timed_region": round(t_wall, 4)}
     print(json.dumps(line), flush=True)

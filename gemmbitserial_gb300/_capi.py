@@ -41,6 +41,17 @@ SIGNATURES = {
     "gbs_export": (i32, [vp, i32, vp, vp]),
     "gbs_get_planes": (i32, [vp, i32, vp, vp]),
     "gbs_set_pipe": (i32, [vp, i32]),
+    "gbs_adjoint": (i32, [vp, vp, vp, vp, vp]),
+    "gbs_fma_peak": (i32, [C.POINTER(C.c_double)]),
+    "gbs_group_create": (i32, [C.POINTER(vp), i32, C.POINTER(vp)]),
+    "gbs_group_import": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(i32), vp]),
+    "gbs_group_gemm": (i32, [vp, vp]),
+    "gbs_group_capture": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(i32), vp]),
+    "gbs_group_replay": (i32, [vp, vp]),
+    "gbs_group_status": (i32, [vp, vp]),
+    "gbs_group_stats": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+    "gbs_group_free": (i32, [vp]),
+    "gbs_debug_group_poison_tile": (i32, [vp, C.c_uint32]),
     "gbs_pipe_peaks": (i32, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gbs_last_error": (C.c_char_p, []),
     "gbs_version": (C.c_char_p, []),

@@ -83,9 +83,13 @@ void free_ctx_buffers(gbs_ctx *c) {
 }
 
 // Epilogue and operand order for one context (see gbs_internal.h: Epilogue).
+}  // namespace
+
 void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum) {
   memset(&e, 0, sizeof(e));
   const bool lb = c->lhs.bipolar(), rb = c->rhs.bipolar();
+  e.neg_i = (c->lhs.issigned && !lb) ? (int)c->lhs.nbits - 1 : -1;
+  e.neg_j = (c->rhs.issigned && !rb) ? (int)c->rhs.nbits - 1 : -1;
   if (lb && rb) {  // arch-generic.hpp:255-259: ncols - 2 * popc(a ^ b)
     e.use_xor = 1;
     e.alpha[0][0] = -2;
@@ -93,6 +97,7 @@ void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum) {
     return;
   }
   const bool mixed = lb != rb;  // arch-generic.hpp:185: alpha doubled, res seeded with -rowsum(regular)
+  e.shift = mixed ? 1 : 0;
   for (uint64_t i = 0; i < c->lhs.nbits; i++) {
     const bool ni = c->lhs.issigned && !lb && i == c->lhs.nbits - 1;
     for (uint64_t j = 0; j < c->rhs.nbits; j++) {
@@ -108,8 +113,6 @@ void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum) {
     else e.ra = rowsum;     // result column m is seeded with -rowsum(lhs row m)
   }
 }
-
-}  // namespace
 
 int choose_pipe(const gbs_ctx *c);
 
@@ -287,6 +290,8 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.wpr = c->lhs.wpr();
   sh.a_plane = c->lhs.nrows_a * sh.wpr;
   sh.b_plane = c->rhs.nrows_a * sh.wpr;
+  sh.a_rows = c->lhs.nrows_a;
+  sh.b_rows = c->rhs.nrows_a;
   sh.wa = (int)c->lhs.nbits;
   sh.wb = (int)c->rhs.nbits;
   const int pipe = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;

@@ -63,11 +63,11 @@ __global__ void __launch_bounds__(NT, 2) gemm_bmma_kernel(GemmShape g, Epilogue 
       const int plane = li / (rows * (KW / 2)), rem = li % (rows * (KW / 2));
       const int row = rem / (KW / 2), c = rem % (KW / 2);
       const uint64_t k = k0 + 2 * c;
-      const uint64_t *src = isA ? g.A + plane * g.a_plane + (m0 + row) * wpr
-                                : g.B + plane * g.b_plane + (n0 + row) * wpr;
+      const uint64_t grow = (isA ? m0 : n0) + row;
+      const uint64_t *base = isA ? g.A + plane * g.a_plane : g.B + plane * g.b_plane;
       const uint32_t dst = s + (isA ? plane * a_tile : wa * a_tile + plane * b_tile) + swz(row, c);
-      const bool ok = k < wpr;
-      cp_async16(dst, ok ? src + k : src, ok);
+      const bool ok = k < wpr && grow < (isA ? g.a_rows : g.b_rows);
+      cp_async16(dst, ok ? base + grow * wpr + k : base, ok);
     }
   };
 

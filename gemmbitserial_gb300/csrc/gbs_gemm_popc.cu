@@ -8,12 +8,15 @@
 // (ncols - 2*xor, arch-generic.hpp:255-259) into one int32 epilogue.  All
 // arithmetic is modulo 2^32, as the reference's int32 accumulators.
 //
-// Two kernels:
-//  * gemm_popc_tiled: 64 x 64 output tile per 256-thread CTA, 4 x 4 outputs
-//    per thread, planes staged through shared memory by cp.async in K chunks
-//    (double buffered).  Thread (tx, ty) owns lhs rows tx + 16i and rhs rows
-//    ty + 16j, so a half-warp stores 16 consecutive results of the
+// Kernels:
+//  * gemm_popc_tiled<BM, BN>: one BM x BN output tile per 256-thread CTA (64x64,
+//    32x128 or 16x256, chosen by the lhs row count), 4 x 4 outputs per
+//    thread, planes staged through shared memory by cp.async in K chunks
+//    (double buffered).  Thread (tx, ty) owns lhs rows tx + (BM/4)i and rhs
+//    rows ty + (BN/4)j, so consecutive lanes store consecutive results of the
 //    transposed output row.
+//  * gemm_popc_grouped: persistent; CTAs pull tiles of many independent
+//    problems from a device queue (atomic counter) and run the same tile code.
 //  * gemm_popc_skinny: one warp per output element, lanes stride over the K
 //    words; for matrix-vector and other small-output shapes.
 #include "gbs_internal.h"
@@ -21,7 +24,7 @@
 namespace gbs {
 namespace {
 
-constexpr int BM = 64, BN = 64, NT = 256;
+constexpr int NT = 256;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool pred) {
   unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -38,32 +41,46 @@ __device__ __forceinline__ uint32_t pc2(ulonglong2 a, ulonglong2 b) {
   return __popcll(a.x & b.x) + __popcll(a.y & b.y);
 }
 
-template <bool XOR, int KC>
-__global__ void __launch_bounds__(NT, 2) gemm_popc_tiled(GemmShape g, Epilogue e) {
+// Everything one output tile needs.
+struct TileArgs {
+  const uint64_t *A, *B;
+  int32_t *C;
+  const int32_t *ra, *rb;
+  uint64_t M, N, wpr, a_plane, b_plane, a_rows, b_rows;
+  int wa, wb, neg_i, neg_j, shift;
+  uint32_t c0;
+};
+
+// One BM x BN output tile over the full K range.  smem must hold
+// 2 * (wa*BM + wb*BN) * (KC+2) words.  Ends with a __syncthreads(), so the
+// caller may reuse smem right away.
+template <int BM, int BN, int KC, bool XOR>
+__device__ __forceinline__ void popc_tile(const TileArgs &g, uint64_t m0, uint64_t n0, uint64_t *smem) {
   constexpr int LDW = KC + 2;  // padded row stride (words): conflict-free 16-byte reads
+  constexpr int TX = BM / 4, TY = BN / 4;
+  static_assert(TX * TY == NT, "4x4 outputs per thread");
   const int wa = g.wa, wb = g.wb;
-  extern __shared__ __align__(16) uint64_t smem[];
   const int stage_words = (wa * BM + wb * BN) * LDW;
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  const uint64_t m0 = (uint64_t)blockIdx.x * BM, n0 = (uint64_t)blockIdx.y * BN;
+  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
   const uint64_t wpr = g.wpr;
   const int nchunks = (int)((wpr + KC - 1) / KC);
 
   auto load_stage = [&](int st, uint64_t k0) {
     uint64_t *s = smem + st * stage_words;
-    const int per_row = KC / 2;  // 16-byte pieces per row
+    constexpr int per_row = KC / 2;  // 16-byte pieces per row
     const int a_pieces = wa * BM * per_row, all = a_pieces + wb * BN * per_row;
     for (int idx = tid; idx < all; idx += NT) {
       const bool isA = idx < a_pieces;
       const int li = isA ? idx : idx - a_pieces;
-      const int plane = li / (BM * per_row), rem = li % (BM * per_row);
+      const int rows = isA ? BM : BN;
+      const int plane = li / (rows * per_row), rem = li % (rows * per_row);
       const int row = rem / per_row, p = rem % per_row;
       const uint64_t k = k0 + 2 * p;
-      const uint64_t *src = isA ? g.A + plane * g.a_plane + (m0 + row) * wpr
-                                : g.B + plane * g.b_plane + (n0 + row) * wpr;
-      uint64_t *dst = s + (isA ? 0 : wa * BM * LDW) + (plane * BM + row) * LDW + 2 * p;
-      const bool ok = k < wpr;
-      cp_async16(dst, ok ? src + k : src, ok);
+      const uint64_t grow = (isA ? m0 : n0) + row;
+      const uint64_t *base = isA ? g.A + plane * g.a_plane : g.B + plane * g.b_plane;
+      uint64_t *dst = s + (isA ? plane * BM : wa * BM + plane * BN) * LDW + row * LDW + 2 * p;
+      const bool ok = k < wpr && grow < (isA ? g.a_rows : g.b_rows);
+      cp_async16(dst, ok ? base + grow * wpr + k : base, ok);
     }
   };
 
@@ -103,15 +120,15 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_tiled(GemmShape g, Epilogue e
         for (int kp = 0; kp < KC / 2; kp++) {
           ulonglong2 a[4], b[4];
 #pragma unroll
-          for (int m = 0; m < 4; m++) a[m] = *reinterpret_cast<const ulonglong2 *>(pa + m * 16 * LDW + 2 * kp);
+          for (int m = 0; m < 4; m++) a[m] = *reinterpret_cast<const ulonglong2 *>(pa + m * TX * LDW + 2 * kp);
 #pragma unroll
-          for (int n = 0; n < 4; n++) b[n] = *reinterpret_cast<const ulonglong2 *>(pb + n * 16 * LDW + 2 * kp);
+          for (int n = 0; n < 4; n++) b[n] = *reinterpret_cast<const ulonglong2 *>(pb + n * TY * LDW + 2 * kp);
 #pragma unroll
           for (int m = 0; m < 4; m++)
 #pragma unroll
             for (int n = 0; n < 4; n++) t[m][n] += pc2<XOR>(a[m], b[n]);
         }
-        const uint32_t al = (uint32_t)e.alpha[i][j];
+        const uint32_t al = alpha_of(i, j, g.neg_i, g.neg_j, g.shift, XOR);
 #pragma unroll
         for (int m = 0; m < 4; m++)
 #pragma unroll
@@ -123,15 +140,64 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_tiled(GemmShape g, Epilogue e
 
 #pragma unroll
   for (int n = 0; n < 4; n++) {
-    const uint64_t gn = n0 + ty + 16 * n;
+    const uint64_t gn = n0 + ty + TY * n;
     if (gn >= g.N) continue;
-    const uint32_t bn = e.c0 - (e.rb ? (uint32_t)e.rb[gn] : 0u);
+    const uint32_t bn = g.c0 - (g.rb ? (uint32_t)g.rb[gn] : 0u);
 #pragma unroll
     for (int m = 0; m < 4; m++) {
-      const uint64_t gm = m0 + tx + 16 * m;
+      const uint64_t gm = m0 + tx + TX * m;
       if (gm >= g.M) continue;
-      const uint32_t v = acc[m][n] + bn - (e.ra ? (uint32_t)e.ra[gm] : 0u);
+      const uint32_t v = acc[m][n] + bn - (g.ra ? (uint32_t)g.ra[gm] : 0u);
       g.C[gn * g.M + gm] = (int32_t)v;
+    }
+  }
+}
+
+template <int BM, int BN, int KC, bool XOR>
+__global__ void __launch_bounds__(NT, 2) gemm_popc_tiled(TileArgs g) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  popc_tile<BM, BN, KC, XOR>(g, (uint64_t)blockIdx.x * BM, (uint64_t)blockIdx.y * BN, smem);
+}
+
+// Persistent grouped GEMM: each CTA takes the next tile from the queue until
+// the queue is drained.  A descriptor that fails validation sets a bit in
+// *err and is skipped (no device fault, no wait).
+__global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *__restrict__ probs, int nprob,
+                                                           const GroupTile *__restrict__ tiles, uint32_t ntiles,
+                                                           uint32_t *counter, uint32_t *err) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  __shared__ uint32_t s_tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t t = s_tile;
+    __syncthreads();
+    if (t >= ntiles) break;
+    const GroupTile tl = tiles[t];
+    if (tl.p >= (uint32_t)nprob || tl.cls > 2) {
+      if (threadIdx.x == 0) atomicOr(err, 1u);
+      continue;
+    }
+    const GroupProblem &P = probs[tl.p];
+    const int bm = tile_bm((int)tl.cls), bn = tile_bn((int)tl.cls);
+    const uint64_t m0 = (uint64_t)tl.mt * bm, n0 = (uint64_t)tl.nt * bn;
+    if (m0 >= P.M || n0 >= P.N || P.wa < 1 || P.wa > kMaxBits || P.wb < 1 || P.wb > kMaxBits) {
+      if (threadIdx.x == 0) atomicOr(err, 2u);
+      continue;
+    }
+    TileArgs g;
+    g.A = P.A; g.B = P.B; g.C = P.C; g.ra = P.ra; g.rb = P.rb;
+    g.M = P.M; g.N = P.N; g.wpr = P.wpr; g.a_plane = P.a_plane; g.b_plane = P.b_plane;
+    g.a_rows = P.a_rows; g.b_rows = P.b_rows;
+    g.wa = P.wa; g.wb = P.wb; g.neg_i = P.neg_i; g.neg_j = P.neg_j; g.shift = P.shift; g.c0 = P.c0;
+    if (P.use_xor) {
+      if (tl.cls == 0) popc_tile<64, 64, kGroupKC, true>(g, m0, n0, smem);
+      else if (tl.cls == 1) popc_tile<32, 128, kGroupKC, true>(g, m0, n0, smem);
+      else popc_tile<16, 256, kGroupKC, true>(g, m0, n0, smem);
+    } else {
+      if (tl.cls == 0) popc_tile<64, 64, kGroupKC, false>(g, m0, n0, smem);
+      else if (tl.cls == 1) popc_tile<32, 128, kGroupKC, false>(g, m0, n0, smem);
+      else popc_tile<16, 256, kGroupKC, false>(g, m0, n0, smem);
     }
   }
 }
@@ -164,34 +230,84 @@ __global__ void __launch_bounds__(256) gemm_popc_skinny(GemmShape g, Epilogue e)
   }
 }
 
-template <bool XOR, int KC>
-cudaError_t run_tiled(const GemmShape &g, const Epilogue &e, cudaStream_t s) {
-  const size_t smem = 2ull * (g.wa * BM + g.wb * BN) * (KC + 2) * sizeof(uint64_t);
-  auto kern = gemm_popc_tiled<XOR, KC>;
+template <int BM, int BN, int KC, bool XOR>
+cudaError_t run_tiled(const TileArgs &t, cudaStream_t s) {
+  const size_t smem = 2ull * (t.wa * BM + t.wb * BN) * (KC + 2) * sizeof(uint64_t);
+  auto kern = gemm_popc_tiled<BM, BN, KC, XOR>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  dim3 grid((unsigned)((g.M + BM - 1) / BM), (unsigned)((g.N + BN - 1) / BN));
-  kern<<<grid, NT, smem, s>>>(g, e);
+  dim3 grid((unsigned)((t.M + BM - 1) / BM), (unsigned)((t.N + BN - 1) / BN));
+  kern<<<grid, NT, smem, s>>>(t);
   count_launch();
   return cudaGetLastError();
 }
 
+template <int BM, int BN, bool XOR>
+cudaError_t run_tiled_kc(const TileArgs &t, cudaStream_t s) {
+  const int rows = t.wa * BM + t.wb * BN;
+  if (rows <= 384) return run_tiled<BM, BN, 16, XOR>(t, s);  // <= 110 KB: 2 CTAs/SM
+  if (rows <= 768) return run_tiled<BM, BN, 8, XOR>(t, s);   // <= 123 KB
+  return run_tiled<BM, BN, 4, XOR>(t, s);                    // <= 2304 rows: <= 221 KB
+}
+
+template <bool XOR>
+cudaError_t run_tiled_cls(int cls, const TileArgs &t, cudaStream_t s) {
+  if (cls == 2) return run_tiled_kc<16, 256, XOR>(t, s);
+  if (cls == 1) return run_tiled_kc<32, 128, XOR>(t, s);
+  return run_tiled_kc<64, 64, XOR>(t, s);
+}
+
 }  // namespace
+
+size_t popc_stage_smem(int cls, int wa, int wb, int kc) {
+  return 2ull * (wa * tile_bm(cls) + wb * tile_bn(cls)) * (kc + 2) * sizeof(uint64_t);
+}
+
+// Tile class for a problem: the narrowest lhs tile that covers M without
+// exceeding the shared-memory cap at the grouped chunk size.
+int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap) {
+  int cls = M <= 16 ? 2 : (M <= 32 ? 1 : 0);
+  while (cls > 0 && popc_stage_smem(cls, wa, wb, kGroupKC) > smem_cap) cls--;
+  return cls;
+}
 
 cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
-  const bool skinny = (g.M * g.N <= 32768) || g.M < 16 || g.N < 16;
+  const bool skinny = (g.M * g.N <= 32768) || g.N < 16 || g.M < 4;
   if (skinny) {
     const uint64_t threads = g.M * g.N * 32;
     gemm_popc_skinny<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(g, e);
     count_launch();
     return cudaGetLastError();
   }
-  if (e.use_xor) return run_tiled<true, 16>(g, e, s);
-  const int planes = g.wa + g.wb;
-  if (planes <= 6) return run_tiled<false, 16>(g, e, s);
-  if (planes <= 12) return run_tiled<false, 8>(g, e, s);
-  return run_tiled<false, 4>(g, e, s);
+  TileArgs t;
+  t.A = g.A; t.B = g.B; t.C = g.C; t.ra = e.ra; t.rb = e.rb;
+  t.M = g.M; t.N = g.N; t.wpr = g.wpr; t.a_plane = g.a_plane; t.b_plane = g.b_plane;
+  t.a_rows = g.a_rows; t.b_rows = g.b_rows;
+  t.wa = g.wa; t.wb = g.wb; t.neg_i = e.neg_i; t.neg_j = e.neg_j; t.shift = e.shift; t.c0 = e.c0;
+  const int cls = popc_tile_class(g.M, g.wa, g.wb, 220 * 1024);
+  if (e.use_xor) return run_tiled_cls<true>(cls, t, s);
+  return run_tiled_cls<false>(cls, t, s);
+}
+
+cudaError_t prepare_gemm_popc_grouped(size_t smem) {
+  return cudaFuncSetAttribute(gemm_popc_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+int grouped_blocks_per_sm(size_t smem) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gemm_popc_grouped, NT, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_gemm_popc_grouped(const GroupProblem *probs, int nprob, const GroupTile *tiles, uint32_t ntiles,
+                                     uint32_t *counter, uint32_t *err, size_t smem, int grid, cudaStream_t s) {
+  gemm_popc_grouped<<<grid, NT, smem, s>>>(probs, nprob, tiles, ntiles, counter, err);
+  count_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace gbs

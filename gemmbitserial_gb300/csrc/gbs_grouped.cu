@@ -1,0 +1,326 @@
+// gbs_grouped.cu -- many independent bit-serial GEMMs in one persistent launch.
+//
+// The reference runs a list of GEMMs as a host loop of gemmBitSerial calls
+// over a vector of contexts (benchmark.cpp:192-206, 217-219).  A group does the
+// same work with
+//   * one grouped pack launch for every operand (optional),
+//   * one grouped row-sum launch when some problem is bipolar x regular,
+//   * one persistent GEMM launch whose CTAs drain a device tile queue (an
+//     atomic counter over a tile table sorted by decreasing cost),
+// and can capture that sequence once into a CUDA graph for replay.  Each
+// problem keeps its own context, so results land in each context's res.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbs_internal.h"
+
+struct gbs_group {
+  int device = 0;
+  std::vector<gbs_ctx *> ctxs;
+  gbs::GroupProblem *d_probs = nullptr;
+  gbs::GroupTile *d_tiles = nullptr;
+  uint32_t ntiles = 0;
+  uint32_t *d_scratch = nullptr;  // [0] tile counter, [1] error bits
+  gbs::PackJob *d_rs_jobs = nullptr;
+  int nrs = 0;
+  uint64_t rs_warps = 0;
+  gbs::PackJob *d_pack_jobs = nullptr;
+  int npack = 0;
+  uint64_t pack_warps = 0;
+  size_t smem = 0;
+  int grid = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace gbs {
+namespace {
+
+// Largest dynamic shared memory per CTA that still lets two CTAs share an SM.
+constexpr size_t kGroupSmemCap = 113 * 1024;
+
+bool device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+void free_group(gbs_group *g) {
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->d_probs) cudaFree(g->d_probs);
+  if (g->d_tiles) cudaFree(g->d_tiles);
+  if (g->d_scratch) cudaFree(g->d_scratch);
+  if (g->d_rs_jobs) cudaFree(g->d_rs_jobs);
+  if (g->d_pack_jobs) cudaFree(g->d_pack_jobs);
+  delete g;
+}
+
+template <typename T>
+cudaError_t upload(T **dst, const std::vector<T> &v) {
+  cudaError_t e = dev_alloc((void **)dst, v.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (v.empty()) return cudaSuccess;
+  return cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+// Builds the pack-job table for (lhs_srcs[p], rhs_srcs[p]) of every problem.
+int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs, const int *dtypes) {
+  std::vector<PackJob> jobs;
+  uint64_t warps = 0;
+  for (size_t p = 0; p < g->ctxs.size(); p++) {
+    for (int side = 0; side < 2; side++) {
+      const void *src = side ? rhs[p] : lhs[p];
+      const int dt = dtypes ? dtypes[2 * p + side] : GBS_I8;
+      if (dt < GBS_I8 || dt > GBS_I32) return fail(GBS_EINVAL, "gbs_group: unknown dtype");
+      const Mat &m = side ? g->ctxs[p]->rhs : g->ctxs[p]->lhs;
+      if (m.nrows_a == 0 || m.wpr() == 0) continue;
+      if (m.nrows * m.ncols && (!src || !device_ptr(src)))
+        return fail(GBS_EINVAL, "gbs_group: sources must be device pointers (problem " + std::to_string(p) + ")");
+      PackJob j;
+      memset(&j, 0, sizeof(j));
+      j.src = src;
+      j.planes = m.planes;
+      j.nrows = m.nrows;
+      j.ncols = m.ncols;
+      j.nrows_a = m.nrows_a;
+      j.wpr = m.wpr();
+      j.nbits = (int)m.nbits;
+      j.issigned = m.issigned;
+      j.dtype = dt;
+      j.vec = (dt == GBS_I8 || dt == GBS_U8) && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0;
+      j.warp0 = warps;
+      warps += m.nrows_a * ((m.wpr() + 7) / 8);
+      jobs.push_back(j);
+    }
+  }
+  if (g->d_pack_jobs) cudaFree(g->d_pack_jobs);
+  g->d_pack_jobs = nullptr;
+  if (upload(&g->d_pack_jobs, jobs) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GBS_ENOMEM, "gbs_group: pack table upload failed");
+  }
+  g->npack = (int)jobs.size();
+  g->pack_warps = warps;
+  return GBS_OK;
+}
+
+cudaError_t enqueue_gemm(gbs_group *g, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(g->d_scratch, 0, sizeof(uint32_t), s);  // tile counter only
+  if (e == cudaSuccess && g->nrs) e = launch_rowsum_grouped(g->d_rs_jobs, g->nrs, g->rs_warps, s);
+  if (e == cudaSuccess && g->ntiles)
+    e = launch_gemm_popc_grouped(g->d_probs, (int)g->ctxs.size(), g->d_tiles, g->ntiles, g->d_scratch,
+                                 g->d_scratch + 1, g->smem, g->grid, s);
+  return e;
+}
+
+}  // namespace
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" {
+
+int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
+  if (!out) return fail(GBS_EINVAL, "gbs_group_create: out is NULL");
+  *out = nullptr;
+  if (count < 0 || (count > 0 && !ctxs)) return fail(GBS_EINVAL, "gbs_group_create: bad context list");
+  gbs_group *g = new gbs_group();
+  if (cudaGetDevice(&g->device) != cudaSuccess) {
+    delete g;
+    return cuda_fail(cudaGetLastError(), "gbs_group_create: no device");
+  }
+  std::vector<GroupProblem> probs;
+  std::vector<GroupTile> tiles;
+  std::vector<uint64_t> cost;
+  std::vector<PackJob> rs;
+  uint64_t rs_warps = 0;
+  size_t smem = 16;
+  for (int p = 0; p < count; p++) {
+    gbs_ctx *c = ctxs[p];
+    if (!c) {
+      delete g;
+      return fail(GBS_EINVAL, "gbs_group_create: context " + std::to_string(p) + " is NULL");
+    }
+    if (c->device != g->device) {
+      delete g;
+      return fail(GBS_EINVAL, "gbs_group_create: contexts must live on the current device");
+    }
+    g->ctxs.push_back(c);
+    Epilogue e;
+    make_epilogue(c, e, c->rowsum);
+    GroupProblem P;
+    memset(&P, 0, sizeof(P));
+    P.A = c->lhs.planes;
+    P.B = c->rhs.planes;
+    P.C = c->res;
+    P.ra = e.ra;
+    P.rb = e.rb;
+    P.M = c->lhs.nrows;
+    P.N = c->rhs.nrows;
+    P.wpr = c->lhs.wpr();
+    P.a_plane = c->lhs.nrows_a * P.wpr;
+    P.b_plane = c->rhs.nrows_a * P.wpr;
+    P.a_rows = c->lhs.nrows_a;
+    P.b_rows = c->rhs.nrows_a;
+    P.wa = (int)c->lhs.nbits;
+    P.wb = (int)c->rhs.nbits;
+    P.use_xor = e.use_xor;
+    P.neg_i = e.neg_i;
+    P.neg_j = e.neg_j;
+    P.shift = e.shift;
+    P.c0 = e.c0;
+    P.cls = popc_tile_class(P.M, P.wa, P.wb, kGroupSmemCap);
+    smem = std::max(smem, popc_stage_smem(P.cls, P.wa, P.wb, kGroupKC));
+    probs.push_back(P);
+    const uint64_t bm = tile_bm(P.cls), bn = tile_bn(P.cls);
+    const uint64_t mt = (P.M + bm - 1) / bm, nt = (P.N + bn - 1) / bn;
+    for (uint64_t i = 0; i < mt; i++)
+      for (uint64_t j = 0; j < nt; j++) {
+        tiles.push_back(GroupTile{(uint32_t)p, (uint32_t)i, (uint32_t)j, (uint32_t)P.cls});
+        cost.push_back((uint64_t)P.wa * P.wb * P.wpr);
+      }
+    if (e.ra || e.rb) {  // bipolar x regular: row sums of the regular operand
+      const Mat &reg = c->lhs.bipolar() ? c->rhs : c->lhs;
+      PackJob j;
+      memset(&j, 0, sizeof(j));
+      j.planes = reg.planes;
+      j.rowsum = c->rowsum;
+      j.nrows = reg.nrows;
+      j.ncols = reg.ncols;
+      j.nrows_a = reg.nrows_a;
+      j.wpr = reg.wpr();
+      j.nbits = (int)reg.nbits;
+      j.issigned = reg.issigned;
+      j.warp0 = rs_warps;
+      rs_warps += reg.nrows;
+      if (reg.nrows) rs.push_back(j);
+    }
+  }
+  // Longest tiles first: the queue then balances like LPT scheduling.
+  std::vector<size_t> order(tiles.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+  std::vector<GroupTile> sorted(tiles.size());
+  for (size_t i = 0; i < order.size(); i++) sorted[i] = tiles[order[i]];
+
+  cudaError_t e = upload(&g->d_probs, probs);
+  if (e == cudaSuccess) e = upload(&g->d_tiles, sorted);
+  if (e == cudaSuccess) e = upload(&g->d_rs_jobs, rs);
+  if (e == cudaSuccess) e = dev_alloc((void **)&g->d_scratch, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(g->d_scratch, 0, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = prepare_gemm_popc_grouped(smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    free_group(g);
+    return fail(GBS_ENOMEM, "gbs_group_create: device allocation or upload failed");
+  }
+  g->ntiles = (uint32_t)sorted.size();
+  g->nrs = (int)rs.size();
+  g->rs_warps = rs_warps;
+  g->smem = smem;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device);
+  g->grid = std::max(1, std::min<int>((int)g->ntiles, sms * grouped_blocks_per_sm(smem)));
+  *out = g;
+  return GBS_OK;
+}
+
+int gbs_group_free(gbs_group *g) {
+  if (!g) return GBS_OK;
+  cudaDeviceSynchronize();
+  free_group(g);
+  return GBS_OK;
+}
+
+int gbs_group_import(gbs_group *g, const void *const *lhs_srcs, const void *const *rhs_srcs, const int *dtypes,
+                     void *stream) {
+  if (!g || !lhs_srcs || !rhs_srcs) return fail(GBS_EINVAL, "gbs_group_import: NULL argument");
+  int rc = build_pack_jobs(g, lhs_srcs, rhs_srcs, dtypes);
+  if (rc != GBS_OK) return rc;
+  cudaError_t e = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_import: pack kernel");
+  for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
+  return GBS_OK;
+}
+
+int gbs_group_gemm(gbs_group *g, void *stream) {
+  if (!g) return fail(GBS_EINVAL, "gbs_group_gemm: group is NULL");
+  for (gbs_ctx *c : g->ctxs)
+    if (!c->lhs.imported || !c->rhs.imported) return fail(GBS_ESTATE, "gbs_group_gemm: import every operand first");
+  cudaError_t e = enqueue_gemm(g, (cudaStream_t)stream);
+  return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_group_gemm");
+}
+
+int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *const *rhs_srcs, const int *dtypes,
+                      void *stream) {
+  if (!g) return fail(GBS_EINVAL, "gbs_group_capture: group is NULL");
+  const bool with_pack = lhs_srcs && rhs_srcs;
+  if (with_pack) {
+    int rc = build_pack_jobs(g, lhs_srcs, rhs_srcs, dtypes);
+    if (rc != GBS_OK) return rc;
+  } else {
+    for (gbs_ctx *c : g->ctxs)
+      if (!c->lhs.imported || !c->rhs.imported)
+        return fail(GBS_ESTATE, "gbs_group_capture: without sources, import every operand first");
+  }
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  g->exec = nullptr;
+  g->graph = nullptr;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: begin capture");
+  cudaError_t ke = cudaSuccess;
+  if (with_pack) ke = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, s);
+  if (ke == cudaSuccess) ke = enqueue_gemm(g, s);
+  e = cudaStreamEndCapture(s, &g->graph);
+  if (ke != cudaSuccess) return cuda_fail(ke, "gbs_group_capture: enqueue");
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: end capture");
+  e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: instantiate");
+  if (with_pack)
+    for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
+  return GBS_OK;
+}
+
+int gbs_group_replay(gbs_group *g, void *stream) {
+  if (!g || !g->exec) return fail(GBS_ESTATE, "gbs_group_replay: capture the group first");
+  cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_replay");
+  count_launch((g->npack ? 1 : 0) + (g->nrs ? 1 : 0) + 1);
+  return GBS_OK;
+}
+
+int gbs_group_status(gbs_group *g, void *stream) {
+  if (!g) return fail(GBS_EINVAL, "gbs_group_status: group is NULL");
+  uint32_t err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, g->d_scratch + 1, sizeof(err), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_status");
+  if (err) return fail(GBS_EINVAL, "gbs_group_status: the grouped kernel rejected tile descriptors (bits " +
+                                       std::to_string(err) + ")");
+  return GBS_OK;
+}
+
+int gbs_group_stats(const gbs_group *g, uint64_t *ntiles, uint64_t *smem_bytes, uint64_t *grid) {
+  if (!g) return fail(GBS_EINVAL, "gbs_group_stats: group is NULL");
+  if (ntiles) *ntiles = g->ntiles;
+  if (smem_bytes) *smem_bytes = g->smem;
+  if (grid) *grid = (uint64_t)g->grid;
+  return GBS_OK;
+}
+
+int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile) {
+  if (!g || tile >= g->ntiles) return fail(GBS_EINVAL, "gbs_debug_group_poison_tile: bad tile");
+  GroupTile bad{0xffffffffu, 0u, 0u, 0u};
+  cudaError_t e = cudaMemcpy(g->d_tiles + tile, &bad, sizeof(bad), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_debug_group_poison_tile");
+}
+
+}  // extern "C"

@@ -9,7 +9,7 @@
 
 namespace gbs {
 
-constexpr uint64_t kRowAlign = 128;  // device row padding (rows of a plane)
+constexpr uint64_t kRowAlign = 256;  // device row padding (rows of a plane): a multiple of every tile's row count
 constexpr uint64_t kColAlign = 256;  // device column padding (bits of a row)
 constexpr int kMaxBits = 8;
 
@@ -32,6 +32,46 @@ struct Epilogue {
   const int32_t *ra;  // per-lhs-row subtrahend or null
   const int32_t *rb;  // per-rhs-row subtrahend or null
   int use_xor;
+  // compact form of alpha used by the tiled CUDA-core kernels (alpha_of)
+  int neg_i, neg_j, shift;
+};
+
+// alpha[i][j] from its compact form: +-2^(i+j+shift), negative iff exactly one
+// of i == neg_i, j == neg_j (the signed MSB planes; -1 for none); -2 for XOR.
+__host__ __device__ inline uint32_t alpha_of(int i, int j, int neg_i, int neg_j, int shift, int use_xor) {
+  if (use_xor) return 0u - 2u;
+  const uint32_t a = 1u << (i + j + shift);
+  return ((i == neg_i) != (j == neg_j)) ? 0u - a : a;
+}
+
+// Output tile classes of the CUDA-core kernels: (rows of lhs) x (rows of rhs).
+// 256 threads, 4 x 4 outputs per thread in every class.
+__host__ __device__ constexpr int tile_bm(int cls) { return cls == 0 ? 64 : (cls == 1 ? 32 : 16); }
+__host__ __device__ constexpr int tile_bn(int cls) { return cls == 0 ? 64 : (cls == 1 ? 128 : 256); }
+
+// One problem of a grouped launch (device resident).
+struct GroupProblem {
+  const uint64_t *A, *B;
+  int32_t *C;
+  const int32_t *ra, *rb;
+  uint64_t M, N, wpr, a_plane, b_plane, a_rows, b_rows;  // a_rows/b_rows: padded rows (nrows_a)
+  int wa, wb, use_xor, neg_i, neg_j, shift;
+  uint32_t c0;
+  int cls;
+};
+
+// One output tile of a grouped launch: problem, tile row/column, class.
+struct GroupTile {
+  uint32_t p, mt, nt, cls;
+};
+
+// One operand of a grouped import / row-sum pass; warp0 = first global warp.
+struct PackJob {
+  const void *src;
+  uint64_t *planes;
+  int32_t *rowsum;
+  uint64_t nrows, ncols, nrows_a, wpr, warp0;
+  int nbits, issigned, dtype, vec;
 };
 
 struct GemmShape {
@@ -40,6 +80,7 @@ struct GemmShape {
   int32_t *C;         // result [N][M]
   uint64_t M, N, wpr;
   uint64_t a_plane, b_plane;  // words per plane (nrows_a * wpr)
+  uint64_t a_rows, b_rows;    // padded rows (nrows_a) of lhs and rhs
   int wa, wb;
 };
 
@@ -58,6 +99,9 @@ struct gbs_ctx {
 
 namespace gbs {
 
+// epilogue of one context (gbs_api.cu)
+void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum);
+
 // error and bookkeeping (gbs_api.cu)
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
@@ -71,6 +115,15 @@ cudaError_t launch_export(const Mat &m, int32_t *dst, cudaStream_t s);
 
 // forward kernels
 cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t s);
+int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap);
+size_t popc_stage_smem(int cls, int wa, int wb, int kc);
+constexpr int kGroupKC = 8;
+cudaError_t prepare_gemm_popc_grouped(size_t smem);
+cudaError_t launch_gemm_popc_grouped(const GroupProblem *probs, int nprob, const GroupTile *tiles, uint32_t ntiles,
+                                     uint32_t *counter, uint32_t *err, size_t smem, int grid, cudaStream_t s);
+int grouped_blocks_per_sm(size_t smem);
+cudaError_t launch_pack_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s);
+cudaError_t launch_rowsum_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s);
 cudaError_t launch_gemm_bmma(const GemmShape &g, const Epilogue &e, cudaStream_t s);
 bool bmma_supported(int wa, int wb, int use_xor);
 

@@ -38,17 +38,13 @@ __device__ __forceinline__ uint32_t nibble(uint32_t x, int b) {
   return ((((x >> b) & 0x01010101u) * 0x00204081u) >> 21) & 0xfu;
 }
 
-// Row-major pack.  One warp covers 512 columns (8 words) of one padded row;
-// lane l owns columns [16l, 16l+16) of that span, i.e. a quarter of word l/4.
-__global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
-                                                     int nbits, uint64_t nrows, uint64_t ncols,
-                                                     uint64_t nrows_a, uint64_t wpr, int vec,
-                                                     uint64_t *__restrict__ planes) {
-  const uint64_t segs = (wpr + 7) / 8;
-  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= nrows_a * segs) return;  // warp-uniform
-  const uint64_t r = warp / segs, seg = warp % segs;
+// Row-major pack of one 512-column segment (8 words) of padded row r by one
+// warp; lane l owns columns [16l, 16l+16) of the segment, i.e. a quarter of
+// word l/4.  Rows >= nrows and columns >= ncols produce zero bits.
+__device__ __forceinline__ void pack_segment(const void *__restrict__ src, int dtype, int bipolar, int nbits,
+                                             uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr,
+                                             int vec, uint64_t *__restrict__ planes, uint64_t r, uint64_t seg,
+                                             int lane) {
   const uint64_t col0 = seg * 512 + (uint64_t)lane * 16;
   uint32_t q[4] = {0u, 0u, 0u, 0u};  // 16 codes, 4 per word, byte j%4 of q[j/4]
   if (r < nrows && col0 < ncols) {
@@ -75,6 +71,41 @@ __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ sr
     v |= __shfl_xor_sync(kFull, v, 1);
     v |= __shfl_xor_sync(kFull, v, 2);
     if ((lane & 3) == 0 && w < wpr) planes[b * plane_words + r * wpr + w] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
+                                                     int nbits, uint64_t nrows, uint64_t ncols,
+                                                     uint64_t nrows_a, uint64_t wpr, int vec,
+                                                     uint64_t *__restrict__ planes) {
+  const uint64_t segs = (wpr + 7) / 8;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= nrows_a * segs) return;  // warp-uniform
+  pack_segment(src, dtype, bipolar, nbits, nrows, ncols, nrows_a, wpr, vec, planes, warp / segs, warp % segs,
+               threadIdx.x & 31);
+}
+
+// Index of the job owning global warp w: the last job with warp0 <= w.
+__device__ __forceinline__ int find_job(const PackJob *jobs, int njobs, uint64_t w) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].warp0 <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Grouped import: one launch packs every operand of a grouped GEMM
+// (row-major sources); global warps are numbered across the jobs.
+__global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ jobs, int njobs, uint64_t total) {
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
+    const PackJob &J = jobs[find_job(jobs, njobs, w)];
+    const uint64_t local = w - J.warp0, segs = (J.wpr + 7) / 8;
+    const bool bip = J.nbits == 1 && J.issigned;
+    pack_segment(J.src, J.dtype, bip ? 1 : 0, J.nbits, J.nrows, J.ncols, J.nrows_a, J.wpr, J.vec, J.planes,
+                 local / segs, local % segs, threadIdx.x & 31);
   }
 }
 
@@ -122,14 +153,10 @@ __global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ sr
     if (b < nbits) planes[b * plane_words + r * wpr + w] = (uint64_t)lo[b] | ((uint64_t)hi[b] << 32);
 }
 
-// sumRows (arch-generic.hpp:6-37): one warp per row.  uint32 arithmetic
+// sumRows (arch-generic.hpp:6-37) of row r by one warp.  uint32 arithmetic
 // reproduces the reference's int32 wrap-around.
-__global__ void __launch_bounds__(256) rowsum_kernel(const uint64_t *__restrict__ planes, int nbits, int issigned,
-                                                     uint64_t nrows, uint64_t ncols, uint64_t nrows_a,
-                                                     uint64_t wpr, int32_t *__restrict__ dst) {
-  const uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= nrows) return;
+__device__ __forceinline__ int32_t row_sum(const uint64_t *__restrict__ planes, int nbits, int issigned,
+                                           uint64_t ncols, uint64_t nrows_a, uint64_t wpr, uint64_t r, int lane) {
   const bool bip = nbits == 1 && issigned;
   uint32_t acc = 0;
   for (int b = 0; b < nbits; b++) {
@@ -143,7 +170,29 @@ __global__ void __launch_bounds__(256) rowsum_kernel(const uint64_t *__restrict_
     acc += cnt;
   }
   if (bip) acc = 2u * acc - (uint32_t)ncols;
-  if (lane == 0) dst[r] = (int32_t)acc;
+  return (int32_t)acc;
+}
+
+__global__ void __launch_bounds__(256) rowsum_kernel(const uint64_t *__restrict__ planes, int nbits, int issigned,
+                                                     uint64_t nrows, uint64_t ncols, uint64_t nrows_a,
+                                                     uint64_t wpr, int32_t *__restrict__ dst) {
+  const uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= nrows) return;
+  const int32_t v = row_sum(planes, nbits, issigned, ncols, nrows_a, wpr, r, lane);
+  if (lane == 0) dst[r] = v;
+}
+
+// Grouped row sums: one warp per row over every job (warp0 counts rows).
+__global__ void __launch_bounds__(256) rowsum_grouped(const PackJob *__restrict__ jobs, int njobs, uint64_t total) {
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
+    const PackJob &J = jobs[find_job(jobs, njobs, w)];
+    const uint64_t r = w - J.warp0;
+    const int32_t v = row_sum(J.planes, J.nbits, J.issigned, J.ncols, J.nrows_a, J.wpr, r, lane);
+    if (lane == 0) J.rowsum[r] = v;
+  }
 }
 
 // exportRegular (gemmbitserial.hpp:313-333): one thread per element.
@@ -183,6 +232,22 @@ cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major,
     pack_colmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
                                                             m.nrows_a, m.wpr(), m.planes);
   }
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s) {
+  if (total_warps == 0 || njobs == 0) return cudaSuccess;
+  const uint64_t blocks = (total_warps + 7) / 8;
+  pack_grouped<<<(unsigned)(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, s>>>(jobs, njobs, total_warps);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rowsum_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s) {
+  if (total_warps == 0 || njobs == 0) return cudaSuccess;
+  const uint64_t blocks = (total_warps + 7) / 8;
+  rowsum_grouped<<<(unsigned)(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, s>>>(jobs, njobs, total_warps);
   count_launch();
   return cudaGetLastError();
 }

@@ -64,6 +64,22 @@ __global__ void __launch_bounds__(256) peak_bmma(const uint64_t *in64, int *out,
   out[blockIdx.x * blockDim.x + t] = s;
 }
 
+// 8 independent FMA chains per thread, all SMs busy.
+__global__ void __launch_bounds__(256) peak_fma(const float *in, float *out, int iters) {
+  float x[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) x[j] = in[(threadIdx.x + j) & 255];
+  const float a = in[1] * 1e-3f, b = in[2] * 1e-3f;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) x[j] = fmaf(x[j], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; j++) s += x[j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
 
 int choose_pipe(const gbs_ctx *) {
@@ -122,5 +138,45 @@ extern "C" int gbs_pipe_peaks(double *popc_bitops, double *bmma_bitops) {
   const double warps = (double)blocks * threads / 32.0;
   if (popc_bitops) *popc_bitops = warps * 32.0 * it_popc * 64.0 * 16.0 * 64.0 / tp;
   if (bmma_bitops) *bmma_bitops = warps * it_bmma * 4.0 * 16.0 * 8.0 * 256.0 / tb;
+  return GBS_OK;
+}
+
+extern "C" int gbs_fma_peak(double *flops) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "gbs_fma_peak: no device");
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8, threads = 256, iters = 8192;
+  float *in = nullptr, *out = nullptr;
+  if (dev_alloc((void **)&in, 256 * 4) != cudaSuccess || dev_alloc((void **)&out, blocks * threads * 4) != cudaSuccess) {
+    cudaGetLastError();
+    if (in) cudaFree(in);
+    return fail(GBS_ENOMEM, "gbs_fma_peak: allocation failed");
+  }
+  float h[256];
+  for (int i = 0; i < 256; i++) h[i] = 1.0f + 0.001f * (float)i;
+  cudaMemcpy(in, h, sizeof(h), cudaMemcpyHostToDevice);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  peak_fma<<<blocks, threads>>>(in, out, 16);
+  cudaDeviceSynchronize();
+  float best = 1e30f;
+  for (int r = 0; r < 3; r++) {
+    cudaEventRecord(e0);
+    peak_fma<<<blocks, threads>>>(in, out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  count_launch(4);
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(in);
+  cudaFree(out);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_fma_peak");
+  if (flops) *flops = 2.0 * blocks * threads * (double)iters * 8.0 / (best * 1e-3);
   return GBS_OK;
 }

@@ -90,3 +90,48 @@ def workload(name: str, seed_index: int = 0):
     A = operand(seed, M, K, wA, eA)
     B = operand(seed + 0x100, N, K, wB, eB)
     return M, K, N, wA, eA != "u", wB, eB != "u", A, B
+
+
+def grouped_mix(seed: int = SEED_BASE + 4, count: int = 512, m_max: int = 256, k_words=(4, 128),
+                n_range=(64, 4096)):
+    """The grouped-GEMM problem mix: a list of (M, K, N, wA, encA, wB, encB).
+
+    M = round(exp(U(0, ln m_max))) in [1, m_max] (log-uniform); K = 64 * U{k_words};
+    N = U{n_range}; wA in {1, 2, 4}, wB in {1, 2, 3, 4}; encoding u / s / b with
+    equal probability.  A bipolar draw forces w = 1.  A signed draw with w = 1
+    becomes w = 2, because a 1-bit signed operand is bipolar by definition in
+    gemmbitserial (gemmbitserial.hpp:74-76).
+    """
+    r = splitmix64(seed, count * 8).reshape(count, 8) >> np.uint64(11)
+    u = r.astype(np.float64) / float(1 << 53)
+    out = []
+    for i in range(count):
+        M = int(min(m_max, max(1, round(np.exp(u[i, 0] * np.log(m_max))))))
+        K = 64 * (k_words[0] + int(u[i, 1] * (k_words[1] - k_words[0] + 1)))
+        N = n_range[0] + int(u[i, 2] * (n_range[1] - n_range[0] + 1))
+        wA = (1, 2, 4)[int(u[i, 3] * 3)]
+        wB = (1, 2, 3, 4)[int(u[i, 4] * 4)]
+        eA = "usb"[int(u[i, 5] * 3)]
+        eB = "usb"[int(u[i, 6] * 3)]
+        if eA == "b":
+            wA = 1
+        elif eA == "s" and wA == 1:
+            wA = 2
+        if eB == "b":
+            wB = 1
+        elif eB == "s" and wB == 1:
+            wB = 2
+        out.append((M, K, N, wA, eA, wB, eB))
+    return out
+
+
+def torch_operand(gen, rows: int, cols: int, bits: int, enc: str, device):
+    """A rows x cols int8 CUDA tensor with the distribution of operand(), drawn by a torch generator."""
+    import torch
+    if enc == "b":
+        return (torch.randint(0, 2, (rows, cols), generator=gen, device=device, dtype=torch.int8) * 2 - 1)
+    if enc == "s":
+        lo, hi = -(1 << (bits - 1)), (1 << (bits - 1)) - 1
+    else:
+        lo, hi = 0, (1 << bits) - 1
+    return torch.randint(lo, hi + 1, (rows, cols), generator=gen, device=device, dtype=torch.int16).to(torch.int8)

@@ -14,7 +14,7 @@
  * Matrix storage on the device keeps the reference's bit-serial layout
  * (gemmbitserial.hpp:50): 64-bit words, [nbits][nrows_a][ncols_a/64], column c
  * of row r in plane b at word c>>6, bit c&63, all padding zero.  The device
- * pads rows to a multiple of 128 and columns to a multiple of 256 (the
+ * pads rows to a multiple of 256 and columns to a multiple of 256 (the
  * reference pads columns to 64, or to 256 for matrix-vector contexts, and
  * rows to its cache block); results never depend on padding.
  */
@@ -137,11 +137,68 @@ GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
 GBS_API int gbs_set_pipe(gbs_ctx *ctx, int pipe);
 
+/* ---- adjoint (quantisation-aware training) ------------------------------ *
+ * No reference counterpart: the reference has no backward pass.  For the
+ * forward res[n*M + m] = sum_k A[m,k] * B[n,k] of an imported context and an
+ * FP32 upstream gradient dC in the same transposed layout (N x M):
+ *   dA[m*K + k] = sum_n dC[n*M + m] * B[n,k]     (M x K, row-major)
+ *   dB[n*K + k] = sum_m dC[n*M + m] * A[m,k]     (N x K, the rhs layout)
+ * with A, B the values the planes encode (bipolar: +-1; signed MSB negative).
+ * FP32 accumulation.  dC, dA, dB are DEVICE pointers; dA or dB may be NULL to
+ * skip that gradient.  Asynchronous on `stream`. */
+GBS_API int gbs_adjoint(gbs_ctx *ctx, const float *dC, float *dA, float *dB, void *stream);
+
+/* ---- grouped GEMM ------------------------------------------------------ *
+ * No single reference counterpart: the reference runs a list of GEMMs as a
+ * host loop of gemmBitSerial over a vector of contexts (benchmark.cpp:192-219).
+ * A group runs the GEMMs of many contexts (any shapes, widths and encodings,
+ * same device) as ONE persistent kernel that drains a device tile queue;
+ * results land in each context's result buffer.  Contexts must outlive the
+ * group and keep their shapes. */
+typedef struct gbs_group gbs_group;
+
+/* Builds the device problem table and the tile queue for ctxs[0..count). */
+GBS_API int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out);
+
+/* importRegular for every operand in one launch: lhs_srcs[p] (M x K) and
+ * rhs_srcs[p] (N x K) are row-major DEVICE pointers; dtypes holds 2*count
+ * GBS_* codes (lhs, rhs per problem) or is NULL for all GBS_I8. */
+GBS_API int gbs_group_import(gbs_group *g, const void *const *lhs_srcs, const void *const *rhs_srcs,
+                             const int *dtypes, void *stream);
+
+/* gemmBitSerial for every problem of the group: one persistent launch (plus
+ * one row-sum launch when some problem is bipolar x regular). */
+GBS_API int gbs_group_gemm(gbs_group *g, void *stream);
+
+/* Captures [grouped import of the given sources] + grouped GEMM into a CUDA
+ * graph held by the group (sources NULL: GEMM only, operands already
+ * imported).  The captured sources are fixed; refill their contents and
+ * replay. */
+GBS_API int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *const *rhs_srcs,
+                              const int *dtypes, void *stream);
+
+/* Launches the captured graph on `stream`. */
+GBS_API int gbs_group_replay(gbs_group *g, void *stream);
+
+/* Reads the device error word of the group (synchronises `stream`):
+ * GBS_EINVAL if the grouped kernel rejected a tile descriptor. */
+GBS_API int gbs_group_status(gbs_group *g, void *stream);
+
+/* Tile count, dynamic shared memory per CTA and persistent grid size. */
+GBS_API int gbs_group_stats(const gbs_group *g, uint64_t *ntiles, uint64_t *smem_bytes, uint64_t *grid);
+
+/* Synchronises the device and frees the group (not its contexts). */
+GBS_API int gbs_group_free(gbs_group *g);
+
 /* Measures the sustained AND+popcount rate (bit operations per second: one
  * bit of one plane pair of one output) of the CUDA-core pipe and of the b1
  * tensor pipe on the current device (~50 ms).  Either pointer may be NULL.
  * No reference counterpart: the reference has a single CPU pipe. */
 GBS_API int gbs_pipe_peaks(double *popc_bitops, double *bmma_bitops);
+
+/* Measures the sustained FP32 FMA rate (FLOP/s, 2 per FMA) of the current
+ * device, the roofline of gbs_adjoint (~20 ms).  No reference counterpart. */
+GBS_API int gbs_fma_peak(double *flops);
 
 /* Message describing the last failure on the calling thread ("" if none). */
 GBS_API const char *gbs_last_error(void);
@@ -153,6 +210,10 @@ GBS_API const char *gbs_version(void);
 
 /* Makes the n-th next allocation made by the library fail (n >= 1); 0 disarms. */
 GBS_API void gbs_debug_fail_alloc_after(int n);
+
+/* Overwrites tile `tile` of a group's queue with an invalid descriptor, to
+ * exercise the grouped kernel's descriptor validation (host-side injection). */
+GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 
 /* Number of kernel launches the library has issued since load (all entry points). */
 GBS_API uint64_t gbs_debug_launch_count(void);

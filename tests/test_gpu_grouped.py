@@ -1,0 +1,140 @@
+"""Grouped GEMM (one persistent launch over many contexts, optionally captured
+with the packing into a CUDA graph): bit-exact per problem against the oracle
+on a reduced mix, and against the plain per-problem GPU path on the full
+512-problem mix."""
+import numpy as np
+import pytest
+
+from gemmbitserial_gb300 import _capi, datagen
+from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext, gemmBitSerial
+from gemmbitserial_gb300.grouped import Group
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib(gbs_lib):
+    import torch
+    assert torch.cuda.is_available()
+    return gbs_lib
+
+
+def make_contexts(mix):
+    return [allocGEMMContext(M, K, N, wA, wB, eA != "u", eB != "u") for (M, K, N, wA, eA, wB, eB) in mix]
+
+
+def test_grouped_reduced_mix_matches_oracle():
+    import torch
+    mix = datagen.grouped_mix(seed=datagen.SEED_BASE + 77, count=96, k_words=(1, 40), n_range=(1, 700))
+    host = []
+    for i, (M, K, N, wA, eA, wB, eB) in enumerate(mix):
+        A = datagen.operand(datagen.SEED_BASE + 1000 + 2 * i, M, K, wA, eA)
+        B = datagen.operand(datagen.SEED_BASE + 1001 + 2 * i, N, K, wB, eB)
+        if i % 5 == 1:  # exercise other element types through the grouped pack
+            A = A.astype(np.int32)
+        if i % 7 == 2 and eB != "b":
+            B = (B.astype(np.int16) & 0xFF).astype(np.uint8) if eB == "u" else B.astype(np.int16)
+        host.append((A, B))
+    ctxs = make_contexts(mix)
+    dev = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in host]
+    s = torch.cuda.Stream()
+    g = Group(ctxs)
+    try:
+        with torch.cuda.stream(s):
+            g.import_([a for a, _ in dev], [b for _, b in dev], stream=s)
+            g.gemm(stream=s)
+        s.synchronize()
+        assert g.status(s) == _capi.GBS_OK
+        for (M, K, N, wA, eA, wB, eB), (A, B), c in zip(mix, host, ctxs):
+            want = O.oracle_gemm(A, B, wA, wB, eA != "u", eB != "u")
+            assert np.array_equal(c.res.reshape(N, M), want), (M, K, N, wA, eA, wB, eB)
+        # the captured graph (pack + gemm) reproduces it, twice in a row
+        with torch.cuda.stream(s):
+            g.capture([a for a, _ in dev], [b for _, b in dev], stream=s)
+            g.replay(stream=s)
+            g.replay(stream=s)
+        s.synchronize()
+        for (M, K, N, wA, eA, wB, eB), (A, B), c in zip(mix, host, ctxs):
+            want = O.oracle_gemm(A, B, wA, wB, eA != "u", eB != "u")
+            assert np.array_equal(c.res.reshape(N, M), want)
+    finally:
+        g.free()
+        for c in ctxs:
+            deallocGEMMContext(c)
+
+
+def test_grouped_full_mix_matches_plain_path():
+    """The 512-problem mix: grouped graph replay == plain per-problem path, and a sample == oracle."""
+    import torch
+    mix = datagen.grouped_mix()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(1234)
+    ops = [(datagen.torch_operand(gen, M, K, wA, eA, "cuda"), datagen.torch_operand(gen, N, K, wB, eB, "cuda"))
+           for (M, K, N, wA, eA, wB, eB) in mix]
+    plain = make_contexts(mix)
+    grouped = make_contexts(mix)
+    s = torch.cuda.Stream()
+    g = Group(grouped)
+    try:
+        with torch.cuda.stream(s):
+            for c, (a, b) in zip(plain, ops):
+                c.lhs.importRegular(a, stream=s)
+                c.rhs.importRegular(b, stream=s)
+                gemmBitSerial(c, stream=s)
+            g.capture([a for a, _ in ops], [b for _, b in ops], stream=s)
+            g.replay(stream=s)
+        s.synchronize()
+        assert g.status(s) == _capi.GBS_OK
+        for i, (cp, cg) in enumerate(zip(plain, grouped)):
+            assert np.array_equal(cp.res, cg.res), mix[i]
+        rng = np.random.default_rng(0)
+        for i in rng.choice(len(mix), 6, replace=False):
+            M, K, N, wA, eA, wB, eB = mix[i]
+            A, B = ops[i][0].cpu().numpy(), ops[i][1].cpu().numpy()
+            want = O.oracle_gemm(A, B, wA, wB, eA != "u", eB != "u", threads=8)
+            assert np.array_equal(grouped[i].res.reshape(N, M), want), mix[i]
+    finally:
+        g.free()
+        for c in plain + grouped:
+            deallocGEMMContext(c)
+
+
+def test_grouped_rejects_bad_descriptors_without_faulting(lib):
+    import torch
+    mix = [(40, 640, 300, 2, "u", 3, "s"), (7, 256, 90, 1, "b", 4, "s")]
+    ctxs = make_contexts(mix)
+    ops = [(torch.ones(M, K, dtype=torch.int8, device="cuda"), torch.ones(N, K, dtype=torch.int8, device="cuda"))
+           for (M, K, N, *_r) in mix]
+    g = Group(ctxs)
+    try:
+        g.import_([a for a, _ in ops], [b for _, b in ops])
+        assert lib.gbs_debug_group_poison_tile(g._h, 0) == _capi.GBS_OK
+        g.gemm()
+        torch.cuda.synchronize()
+        assert g.status() == _capi.GBS_EINVAL
+        assert b"rejected" in lib.gbs_last_error()
+        # the context stays usable
+        res = torch.zeros(1, device="cuda")
+        assert float((res + 1).item()) == 1.0
+    finally:
+        g.free()
+        for c in ctxs:
+            deallocGEMMContext(c)
+
+
+def test_grouped_rejects_host_sources():
+    mix = [(4, 64, 4, 1, "u", 1, "u")]
+    ctxs = make_contexts(mix)
+    g = Group(ctxs)
+    try:
+        import ctypes as C
+        A = np.ones((4, 64), np.int8)
+        L = (C.c_void_p * 1)(A.ctypes.data)
+        rc = _capi.load().gbs_group_import(g._h, L, L, None, None)
+        assert rc == _capi.GBS_EINVAL
+        with pytest.raises(_capi.GBSError):
+            g.gemm()  # nothing imported yet
+    finally:
+        g.free()
+        deallocGEMMContext(ctxs[0])
