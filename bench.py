@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-problem measurement")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     return p.parse_args()
 
 
@@ -266,6 +267,77 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2):
             "mix": "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
 
 
+def measure_adjoint(lib, dev, stream, reps=10, warmup=3):
+    """QAT layer adjoint: A 4096x2048 u2, B 2048x2048 bipolar, dC ~ N(0,1).  Ours (FP32 from the packed
+    planes) vs the plain GPU path (export values, two FP32 cuBLAS matmuls with TF32 off)."""
+    import torch
+    from gemmbitserial_gb300 import _capi, datagen
+    from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext
+    from oracle import oracle as O
+    M, K, N = 4096, 2048, 2048
+    A = datagen.operand(datagen.SEED_BASE + 50, M, K, 2, "u")
+    B = datagen.operand(datagen.SEED_BASE + 51, N, K, 1, "b")
+    dC = datagen.normal_f32(datagen.SEED_BASE + 52, (N, M))
+    ctx = allocGEMMContext(M, K, N, 2, 1, False, True)
+    sh = C.c_void_p(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        ctx.lhs.importRegular(torch.from_numpy(A).to(dev), stream=stream)
+        ctx.rhs.importRegular(torch.from_numpy(B).to(dev), stream=stream)
+        d = torch.from_numpy(dC).to(dev)
+        dA = torch.empty(M, K, device=dev)
+        dB = torch.empty(N, K, device=dev)
+        Ai = torch.empty(M, K, dtype=torch.int32, device=dev)
+        Bi = torch.empty(N, K, dtype=torch.int32, device=dev)
+    stream.synchronize()
+
+    def ours():
+        _capi.check(lib.gbs_adjoint(ctx._h, C.c_void_p(d.data_ptr()), C.c_void_p(dA.data_ptr()),
+                                    C.c_void_p(dB.data_ptr()), sh))
+
+    prev_tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+
+    def plain():
+        _capi.check(lib.gbs_export(ctx._h, 0, C.c_void_p(Ai.data_ptr()), sh))
+        _capi.check(lib.gbs_export(ctx._h, 1, C.c_void_p(Bi.data_ptr()), sh))
+        pa = d.T @ Bi.float()
+        pb = d @ Ai.float()
+        return pa, pb
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                fn()
+            stream.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_ours = timed(ours)
+    t_plain = timed(plain)
+    torch.backends.cuda.matmul.allow_tf32 = prev_tf32
+    fma = C.c_double()
+    _capi.check(lib.gbs_fma_peak(C.byref(fma)))
+    dA64, dB64 = O.adjoint_fp64(dC, O.decode_values(A, 2, False), O.decode_values(B, 1, True))
+    ea = float(np.max(np.abs(dA.cpu().numpy() - dA64)) / np.max(np.abs(dA64)))
+    eb = float(np.max(np.abs(dB.cpu().numpy() - dB64)) / np.max(np.abs(dB64)))
+    deallocGEMMContext(ctx)
+    flops = 2.0 * 2.0 * M * K * N
+    achieved = flops / (t_ours * 1e-3) / 1e12
+    return {"shape": f"A {M}x{K} u2, B {N}x{K} bipolar, dC {N}x{M} fp32", "ms": round(t_ours, 4),
+            "tflops": round(achieved, 2), "plain_ms": round(t_plain, 4),
+            "plain": "export values + 2 FP32 cuBLAS matmuls (TF32 off)",
+            "speedup_vs_plain": round(t_plain / t_ours, 3),
+            "roofline": {"bound": "fp32 fma", "achieved": round(achieved, 2), "peak": round(fma.value / 1e12, 2),
+                         "unit": "TFLOP/s", "frac": round(achieved / (fma.value / 1e12), 4),
+                         "peak_source": "measured in-process (gbs_fma_peak)"},
+            "max_rel_err_normwise": {"dA": ea, "dB": eb}}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -376,6 +448,7 @@ def run_ours(args):
     clocks = clk.summary()
 
     grouped = None if args.no_grouped else measure_grouped(lib, dev, stream)
+    adjoint = None if args.no_adjoint else measure_adjoint(lib, dev, stream)
 
     cpu = None
     if not args.no_cpu_baseline and world == 1:
@@ -398,7 +471,7 @@ def run_ours(args):
                          "peak_source": "measured in-process (gbs_pipe_peaks: CUDA-core AND+POPC loop)",
                          "bmma_peak": round(2.0 * bmma.value / 1e12, 3),
                          "traffic": traffic, "algorithmic_bytes": int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)},
-            "grouped": grouped,
+            "grouped": grouped, "adjoint": adjoint,
             "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
             "wall_s_timed_region": round(t_wall, 4)}
     print(json.dumps(line), flush=True)

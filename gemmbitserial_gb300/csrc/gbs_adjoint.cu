@@ -39,7 +39,7 @@ __device__ __forceinline__ float x_at(const AdjArgs &a, uint64_t s, uint64_t r) 
 }
 
 template <bool DA>
-__global__ void __launch_bounds__(NT, 2) adjoint_kernel(AdjArgs a) {
+__global__ void __launch_bounds__(NT, 1) adjoint_kernel(AdjArgs a) {
   __shared__ __align__(16) float sX[2][BS][BR];
   __shared__ __align__(16) float sV[2][BS][BKc];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -115,11 +115,16 @@ __global__ void __launch_bounds__(NT, 2) adjoint_kernel(AdjArgs a) {
     *reinterpret_cast<float4 *>(&sV[st][tid >> 5][(tid & 31) * 4]) = make_float4(v[0], v[1], v[2], v[3]);
   };
 
-  float acc[8][8];
+  // Two-level FP32 accumulation: FMAs go into part[][] for kFold stages (32
+  // reduction terms), which is then added into acc[][].  The running sum then
+  // sees S/32 roundings instead of S, which keeps the normwise error of a
+  // 2048-4096 term reduction near 3e-7 of the largest result.
+  constexpr int kFold = 4;
+  float acc[8][8], part[8][8];
 #pragma unroll
   for (int i = 0; i < 8; i++)
 #pragma unroll
-    for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+    for (int j = 0; j < 8; j++) acc[i][j] = part[i][j] = 0.f;
 
   float xt[4];
   uint32_t vb[kMaxBits];
@@ -148,7 +153,16 @@ __global__ void __launch_bounds__(NT, 2) adjoint_kernel(AdjArgs a) {
 #pragma unroll
       for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int j = 0; j < 8; j++) acc[i][j] = fmaf(xr[i], vk[j], acc[i][j]);
+        for (int j = 0; j < 8; j++) part[i][j] = fmaf(xr[i], vk[j], part[i][j]);
+    }
+    if ((c + 1) % kFold == 0 || !more) {
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          acc[i][j] += part[i][j];
+          part[i][j] = 0.f;
+        }
     }
     if (more) {
       store_x(st ^ 1, xt);

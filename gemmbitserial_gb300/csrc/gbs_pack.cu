@@ -41,12 +41,12 @@ __device__ __forceinline__ uint32_t nibble(uint32_t x, int b) {
 // Row-major pack of one 512-column segment (8 words) of padded row r by one
 // warp; lane l owns columns [16l, 16l+16) of the segment, i.e. a quarter of
 // word l/4.  Rows >= nrows and columns >= ncols produce zero bits.
-__device__ __forceinline__ void pack_segment(const void *__restrict__ src, int dtype, int bipolar, int nbits,
-                                             uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr,
-                                             int vec, uint64_t *__restrict__ planes, uint64_t r, uint64_t seg,
-                                             int lane) {
+// load_codes fetches the lane's 16 codes; emit_planes gathers and stores them.
+__device__ __forceinline__ void load_codes(const void *__restrict__ src, int dtype, int bipolar, uint64_t nrows,
+                                           uint64_t ncols, int vec, uint64_t r, uint64_t seg, int lane,
+                                           uint32_t (&q)[4]) {
   const uint64_t col0 = seg * 512 + (uint64_t)lane * 16;
-  uint32_t q[4] = {0u, 0u, 0u, 0u};  // 16 codes, 4 per word, byte j%4 of q[j/4]
+  q[0] = q[1] = q[2] = q[3] = 0u;  // 16 codes, 4 per word, byte j%4 of q[j/4]
   if (r < nrows && col0 < ncols) {
     const uint64_t base = r * ncols + col0;
     if (vec) {  // 1-byte elements, 16-byte aligned rows
@@ -63,6 +63,10 @@ __device__ __forceinline__ void pack_segment(const void *__restrict__ src, int d
       }
     }
   }
+}
+
+__device__ __forceinline__ void emit_planes(int nbits, uint64_t nrows_a, uint64_t wpr, uint64_t *__restrict__ planes,
+                                            uint64_t r, uint64_t seg, int lane, const uint32_t (&q)[4]) {
   const uint64_t w = seg * 8 + (lane >> 2);
   const uint64_t plane_words = nrows_a * wpr;
   for (int b = 0; b < nbits; b++) {
@@ -72,6 +76,15 @@ __device__ __forceinline__ void pack_segment(const void *__restrict__ src, int d
     v |= __shfl_xor_sync(kFull, v, 2);
     if ((lane & 3) == 0 && w < wpr) planes[b * plane_words + r * wpr + w] = v;
   }
+}
+
+__device__ __forceinline__ void pack_segment(const void *__restrict__ src, int dtype, int bipolar, int nbits,
+                                             uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr,
+                                             int vec, uint64_t *__restrict__ planes, uint64_t r, uint64_t seg,
+                                             int lane) {
+  uint32_t q[4];
+  load_codes(src, dtype, bipolar, nrows, ncols, vec, r, seg, lane, q);
+  emit_planes(nbits, nrows_a, wpr, planes, r, seg, lane, q);
 }
 
 __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
@@ -97,15 +110,42 @@ __device__ __forceinline__ int find_job(const PackJob *jobs, int njobs, uint64_t
 }
 
 // Grouped import: one launch packs every operand of a grouped GEMM
-// (row-major sources); global warps are numbered across the jobs.
+// (row-major sources); global segment units are numbered across the jobs.
+// A warp takes kRun consecutive units per step: one job lookup, then the
+// loads of kPar units are in flight together before any of them is packed.
+constexpr int kRun = 16, kPar = 4;
+
 __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ jobs, int njobs, uint64_t total) {
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw) {
-    const PackJob &J = jobs[find_job(jobs, njobs, w)];
-    const uint64_t local = w - J.warp0, segs = (J.wpr + 7) / 8;
-    const bool bip = J.nbits == 1 && J.issigned;
-    pack_segment(J.src, J.dtype, bip ? 1 : 0, J.nbits, J.nrows, J.ncols, J.nrows_a, J.wpr, J.vec, J.planes,
-                 local / segs, local % segs, threadIdx.x & 31);
+  const int lane = threadIdx.x & 31;
+  for (uint64_t base = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRun; base < total;
+       base += nw * kRun) {
+    int j = find_job(jobs, njobs, base);
+    for (int u0 = 0; u0 < kRun; u0 += kPar) {
+      uint32_t q[kPar][4];
+      int jj[kPar];
+      uint64_t rr[kPar], ss[kPar];
+#pragma unroll
+      for (int u = 0; u < kPar; u++) {
+        const uint64_t w = base + u0 + u;
+        jj[u] = -1;
+        q[u][0] = q[u][1] = q[u][2] = q[u][3] = 0u;
+        if (w >= total) continue;
+        while (j + 1 < njobs && jobs[j + 1].warp0 <= w) j++;
+        const PackJob &J = jobs[j];
+        const uint64_t local = w - J.warp0, segs = (J.wpr + 7) / 8;
+        jj[u] = j;
+        rr[u] = local / segs;
+        ss[u] = local % segs;
+        load_codes(J.src, J.dtype, J.nbits == 1 && J.issigned, J.nrows, J.ncols, J.vec, rr[u], ss[u], lane, q[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kPar; u++) {
+        if (jj[u] < 0) continue;
+        const PackJob &J = jobs[jj[u]];
+        emit_planes(J.nbits, J.nrows_a, J.wpr, J.planes, rr[u], ss[u], lane, q[u]);
+      }
+    }
   }
 }
 
@@ -238,7 +278,7 @@ cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major,
 
 cudaError_t launch_pack_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s) {
   if (total_warps == 0 || njobs == 0) return cudaSuccess;
-  const uint64_t blocks = (total_warps + 7) / 8;
+  const uint64_t blocks = (total_warps + 8 * kRun - 1) / (8 * kRun);
   pack_grouped<<<(unsigned)(blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, s>>>(jobs, njobs, total_warps);
   count_launch();
   return cudaGetLastError();
