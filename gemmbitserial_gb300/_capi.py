@@ -41,6 +41,8 @@ SIGNATURES = {
     "gbs_export": (i32, [vp, i32, vp, vp]),
     "gbs_get_planes": (i32, [vp, i32, vp, vp]),
     "gbs_set_pipe": (i32, [vp, i32]),
+    "gbs_gemm_noalloc": (i32, [vp, i32, vp, i32, u64, u64, u64, u64, u64, i32, i32, vp, vp]),
+    "gbs_noalloc_scratch_bytes": (u64, []),
     "gbs_adjoint": (i32, [vp, vp, vp, vp, vp]),
     "gbs_fma_peak": (i32, [C.POINTER(C.c_double)]),
     "gbs_group_create": (i32, [C.POINTER(vp), i32, C.POINTER(vp)]),

@@ -137,6 +137,29 @@ GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
 GBS_API int gbs_set_pipe(gbs_ctx *ctx, int pipe);
 
+/* ---- one-shot GEMM without allocation ---------------------------------- *
+ * No counterpart in the reference.  For callers that cannot let the library
+ * call cudaMalloc -- code running while a stream is captured into a CUDA
+ * graph in global capture mode, real-time loops that must not enter the
+ * allocator, hosts with a fixed memory budget -- this computes
+ * gemmBitSerial of device inputs straight into a device result:
+ *   res[n*M + m] = sum_k A[m*K + k] * B[n*K + k]   (bit-exact, int32 wrap)
+ * with lhs = A (M x K) and rhs = B (N x K) row-major DEVICE arrays of the
+ * given GBS_* element types, encoded as in gbs_import.  It allocates nothing:
+ * the packed planes and row sums live in one fixed file-scope device array of
+ * gbs_noalloc_scratch_bytes() bytes (16 MiB), which every GPU that loads the
+ * library holds until exit.  A GEMM whose packed operands do not fit is
+ * rejected with GBS_EINVAL.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU (other streams
+ * or host threads) race, so order them on one stream. */
+GBS_API int gbs_gemm_noalloc(const void *lhs, int lhs_dtype, const void *rhs, int rhs_dtype, uint64_t M,
+                             uint64_t K, uint64_t N, uint64_t lhsBits, uint64_t rhsBits, int lhsSigned,
+                             int rhsSigned, int32_t *res, void *stream);
+
+/* Size in bytes of the fixed device array gbs_gemm_noalloc works in. */
+GBS_API uint64_t gbs_noalloc_scratch_bytes(void);
+
 /* ---- adjoint (quantisation-aware training) ------------------------------ *
  * No reference counterpart: the reference has no backward pass.  For the
  * forward res[n*M + m] = sum_k A[m,k] * B[n,k] of an imported context and an
