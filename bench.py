@@ -436,15 +436,33 @@ def run_ours(args):
 
     if rank != 0:
         return
-    # ---- roofline of the forward kernel against the measured POPC pipe peak
-    popc, bmma = C.c_double(), C.c_double()
-    _capi.check(lib.gbs_pipe_peaks(C.byref(popc), C.byref(bmma)))
+    # ---- roofline of the forward kernel against the measured peak of the pipe it ran on
     kpad = (K + 63) // 64 * 64
-    binops = 2.0 * M * N * kpad * wA * wB  # AND + add per bit of each plane pair
-    achieved = binops / (ms * 1e-3) / 1e12
-    peak = 2.0 * popc.value / 1e12
-    kernel = "gemm_popc_tiled"
-    traffic = read_traffic(kernel, args.workload)
+    if pipe == _capi.GBS_PIPE_TC:
+        f8, bf16 = C.c_double(), C.c_double()
+        _capi.check(lib.gbs_tc_peaks(C.byref(f8), C.byref(bf16)))
+        kernel = "gemm_tc_kernel"
+        work = 2.0 * M * N * K * wA * wB  # fp8 plane-pair multiply-adds on the tensor pipe
+        achieved = work / (ms * 1e-3) / 1e12
+        peak = f8.value / 1e12
+        roof = {"bound": "tensor", "kernel": kernel, "achieved": round(achieved, 2), "peak": round(peak, 2),
+                "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                "peak_source": "measured in-process (gbs_tc_peaks: tcgen05.mma kind::f8f6f4, M=128 N=256)",
+                "work": "2*M*N*K*wA*wB fp8 plane-pair FLOPs",
+                "bf16_peak_measured": round(bf16.value / 1e12, 1)}
+    else:
+        popc, bmma = C.c_double(), C.c_double()
+        _capi.check(lib.gbs_pipe_peaks(C.byref(popc), C.byref(bmma)))
+        kernel = "gemm_popc_tiled"
+        binops = 2.0 * M * N * kpad * wA * wB  # AND + add per bit of each plane pair
+        achieved = binops / (ms * 1e-3) / 1e12
+        peak = 2.0 * popc.value / 1e12
+        roof = {"bound": "popc", "kernel": kernel, "achieved": round(achieved, 3), "peak": round(peak, 3),
+                "unit": "Tbinop/s", "frac": round(achieved / peak, 4),
+                "peak_source": "measured in-process (gbs_pipe_peaks: CUDA-core AND+POPC loop)",
+                "bmma_peak": round(2.0 * bmma.value / 1e12, 3)}
+    roof["traffic"] = read_traffic(kernel, args.workload)
+    roof["algorithmic_bytes"] = int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)
     clocks = clk.summary()
 
     grouped = None if args.no_grouped else measure_grouped(lib, dev, stream)
@@ -461,16 +479,12 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded splitmix64)",
             "config": dict(desc, parallelism=f"replicas x{world}", l2="flushed before every step (256 MiB write, outside the timed events)",
-                           pipe={1: "popc", 2: "bmma"}.get(pipe, str(pipe))),
+                           pipe={1: "popc", 2: "bmma", 3: "tcgen05"}.get(pipe, str(pipe))),
             "parity": parity,
             "e2e": {"value": round(gops(M, K, N, e2e_s) * world, 3), "unit": "GOPS",
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),
                     "ms_per_step": round(e2e_s * 1e3, 4), "parity": "bit-exact" if e2e_ok else "MISMATCH"},
-            "roofline": {"bound": "popc", "kernel": kernel, "achieved": round(achieved, 3), "peak": round(peak, 3),
-                         "unit": "Tbinop/s", "frac": round(achieved / peak, 4),
-                         "peak_source": "measured in-process (gbs_pipe_peaks: CUDA-core AND+POPC loop)",
-                         "bmma_peak": round(2.0 * bmma.value / 1e12, 3),
-                         "traffic": traffic, "algorithmic_bytes": int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)},
+            "roofline": roof,
             "grouped": grouped, "adjoint": adjoint,
             "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
             "wall_s_timed_region": round(t_wall, 4)}

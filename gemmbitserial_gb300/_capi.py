@@ -13,7 +13,7 @@ from . import build as _build
 GBS_OK, GBS_EINVAL, GBS_ENOMEM, GBS_ECUDA, GBS_ESTATE, GBS_ETIMEOUT, GBS_EUNSUPPORTED = range(7)
 GBS_I8, GBS_U8, GBS_I16, GBS_I32 = range(4)
 GBS_LHS, GBS_RHS = 0, 1
-GBS_PIPE_AUTO, GBS_PIPE_POPC, GBS_PIPE_BMMA = 0, 1, 2
+GBS_PIPE_AUTO, GBS_PIPE_POPC, GBS_PIPE_BMMA, GBS_PIPE_TC = 0, 1, 2, 3
 
 # Every entry point include/gbs.h declares, with (restype, argtypes).
 u64, i32, vp = C.c_uint64, C.c_int, C.c_void_p
@@ -45,6 +45,7 @@ SIGNATURES = {
     "gbs_noalloc_scratch_bytes": (u64, []),
     "gbs_adjoint": (i32, [vp, vp, vp, vp, vp]),
     "gbs_fma_peak": (i32, [C.POINTER(C.c_double)]),
+    "gbs_tc_peaks": (i32, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gbs_group_create": (i32, [C.POINTER(vp), i32, C.POINTER(vp)]),
     "gbs_group_import": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(i32), vp]),
     "gbs_group_gemm": (i32, [vp, vp]),
@@ -59,6 +60,7 @@ SIGNATURES = {
     "gbs_version": (C.c_char_p, []),
     "gbs_debug_fail_alloc_after": (None, [i32]),
     "gbs_debug_launch_count": (u64, []),
+    "gbs_debug_tc_error": (C.c_uint32, []),
 }
 
 _lib = None

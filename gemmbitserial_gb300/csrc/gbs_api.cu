@@ -116,6 +116,14 @@ void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum) {
 
 int choose_pipe(const gbs_ctx *c);
 
+// The pipe gbs_gemm will actually run: a forced tensor-core pipe falls back to
+// the CUDA cores for shapes it does not cover.
+int effective_pipe(const gbs_ctx *c) {
+  const int p = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
+  if (p == GBS_PIPE_TC && !tc_supported(c)) return GBS_PIPE_POPC;
+  return p;
+}
+
 }  // namespace gbs
 
 using namespace gbs;
@@ -129,6 +137,10 @@ const char *gbs_last_error(void) { return g_last_error.c_str(); }
 void gbs_debug_fail_alloc_after(int n) { g_fail_alloc_countdown.store(n > 0 ? n : 0); }
 
 uint64_t gbs_debug_launch_count(void) { return g_launches.load(); }
+
+uint32_t gbs_debug_tc_error(void) { return tc_error_word(); }
+
+int gbs_tc_peaks(double *f8_flops, double *bf16_flops) { return tc_peaks(f8_flops, bf16_flops); }
 
 int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB,
                   gbs_ctx **out) {
@@ -212,7 +224,7 @@ int gbs_ctx_get_info(const gbs_ctx *c, gbs_ctx_info *info) {
   info->lhsBlock = c->lhsBlock;
   info->rhsBlock = c->rhsBlock;
   info->res = c->res;
-  info->pipe = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
+  info->pipe = effective_pipe(c);
   return GBS_OK;
 }
 
@@ -259,7 +271,7 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
 
 int gbs_set_pipe(gbs_ctx *c, int pipe) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_pipe: ctx is NULL");
-  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_BMMA) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
+  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_TC) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
   c->pipe = pipe;
   return GBS_OK;
 }
@@ -294,9 +306,11 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.b_rows = c->rhs.nrows_a;
   sh.wa = (int)c->lhs.nbits;
   sh.wb = (int)c->rhs.nbits;
-  const int pipe = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
+  const int pipe = effective_pipe(c);
   cudaError_t ke;
-  if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
+  if (pipe == GBS_PIPE_TC) {
+    ke = launch_gemm_tc(c, s);
+  } else if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
     if (e.use_xor) {
       // ncols - 2*popc(a^b) = 4*popc(a&b) - rsA - rsB - ncols, rs = bipolar row sums (2*popc - ncols)
       e.use_xor = 0;

@@ -1,0 +1,498 @@
+// gbs_gemm_tc.cu -- forward bit-serial GEMM on the 5th-generation tensor cores
+// (tcgen05.mma, TMEM accumulator, TMA staging).
+//
+// Every plane pair (i, j) is evaluated on the tensor pipe as a product of
+// 0/1 matrices: a set bit of lhs plane i becomes the fp8 (e4m3) value
+// s_i * 2^i and a set bit of rhs plane j becomes t_j * 2^j (s, t = -1 for a
+// signed MSB plane, gemmbitserial.hpp:313-333 / arch-generic.hpp:179-192), a
+// clear bit becomes 0; a bipolar plane becomes +-1.  One fp32 accumulator in
+// TMEM then sums all wA x wB plane-pair products, i.e. the AND + popcount of
+// every plane pair weighted by +-2^(i+j) -- and, because bipolar values are
+// +-1 directly, the bipolar corrections of arch-generic.hpp:45-71, 255-259
+// need no epilogue term.  Every product and partial sum is an integer, exact
+// in fp32 while |sum| < 2^24; the host only selects this kernel when
+// K * max|a| * max|b| < 2^24, so the int32 result is bit-exact.
+//
+// CTA: one 128 x 128 output tile; K advances 128 bits per stage.
+//   warp 0     TMA producer: packed planes of the stage (wA + wB boxes of
+//              128 rows x 16 bytes) into a 4-slot ring, mbarrier complete_tx
+//   warp 1     allocates 128 TMEM columns; lane 0 issues tcgen05.mma
+//              (M=128, N=128, K=32 e4m3) for every plane pair and K step,
+//              tcgen05.commit frees operand slots and finally signals the
+//              accumulator
+//   warps 2-9  decode packed bits into the operand ring (128-byte-swizzled,
+//              K-major canonical layout), then run the epilogue:
+//              tcgen05.ld 32 lanes x 32 columns, fp32 -> int32, coalesced
+//              stores of the transposed result res[n*M + m]
+// Every mbarrier wait is bounded: on timeout the CTA raises g_tc_error,
+// stops issuing work, waits (bounded) for what it issued and frees TMEM.
+#include <cuda.h>
+
+#include <cstring>
+
+#include "gbs_internal.h"
+
+namespace gbs {
+
+static __device__ uint32_t g_tc_error;
+
+namespace {
+
+constexpr int kBM = 128, kBN = 128;
+constexpr int kOpTile = 128 * 128;  // bytes of one plane's operand tile (128 rows x 128 e4m3)
+constexpr int kPkTile = 128 * 16;   // bytes of one plane's packed stage (128 rows x 128 bits)
+constexpr int kDecWarps = 8;
+constexpr int kThreads = 64 + 32 * kDecWarps;
+constexpr int kPkSlots = 4;
+constexpr uint32_t kWaitLimit = 1u << 20;
+
+struct TcArgs {
+  int32_t *C;
+  uint64_t M, N, K;
+  uint32_t nstages;         // K stages of 128 bits
+  uint32_t a_rows, b_rows;  // padded rows per plane (TMA row coordinate of plane i = i * rows + tile row)
+  int wa, wb, a_bip, b_bip, no;
+  uint32_t a_code, b_code;  // packed e4m3 codes of a set bit, one byte per plane (planes 0..3)
+  uint32_t idesc;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: true when the phase completed; false on abort or timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    if (mbar_try(bar, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  atomicOr(&g_tc_error, 1u);
+  return false;
+}
+// Bounded wait that ignores the abort flag: drains work this thread issued.
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it)
+    if (mbar_try(bar, parity)) return;
+  atomicOr(&g_tc_error, 2u);
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+// 4 bits -> 4 bytes holding 0 or 1 (bit i -> byte i); the multiply places the
+// bits at 0..3, 7..10, 14..17, 21..24 without carries, the mask keeps 0, 8, 16, 24.
+__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
+
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int planes = a.wa + a.wb;
+  const uint32_t op_stage = planes * kOpTile, pk_stage = planes * kPkTile;
+  uint8_t *op_ring = smem;
+  uint8_t *pk_ring = op_ring + a.no * op_stage;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(pk_ring + kPkSlots * pk_stage);
+  // barriers: pk_full[4], pk_empty[4], op_full[no], op_empty[no], acc_full, mma_done
+  const uint32_t pk_full = smem_u32(bars), pk_empty = pk_full + 8 * kPkSlots;
+  const uint32_t op_full = pk_empty + 8 * kPkSlots, op_empty = op_full + 8 * a.no;
+  const uint32_t acc_full = op_empty + 8 * a.no, mma_done = acc_full + 8;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kPkSlots + 2 * a.no + 2);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const uint64_t m0 = (uint64_t)blockIdx.x * kBM, n0 = (uint64_t)blockIdx.y * kBN;
+
+  if (tid == 0) {
+    for (int i = 0; i < kPkSlots; i++) {
+      mbar_init(pk_full + 8 * i, 1);                   // producer's expect_tx + TMA bytes
+      mbar_init(pk_empty + 8 * i, 32 * kDecWarps);     // every decoder thread has read the slot
+    }
+    for (int i = 0; i < a.no; i++) {
+      mbar_init(op_full + 8 * i, 32 * kDecWarps);      // every decoder thread has written its rows
+      mbar_init(op_empty + 8 * i, 1);                  // tcgen05.commit of the MMAs that read the slot
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer
+    if (lane == 0) {
+      uint32_t issued = 0;
+      for (uint32_t k = 0; k < a.nstages; k++) {
+        const uint32_t s = k % kPkSlots, use = k / kPkSlots;
+        if (use > 0 && !mbar_wait(pk_empty + 8 * s, (use - 1) & 1, abort_flag)) break;
+        mbar_expect_tx(pk_full + 8 * s, pk_stage);
+        const uint32_t dst = smem_u32(pk_ring + s * pk_stage);
+        for (int i = 0; i < a.wa; i++)
+          tma_load_2d(dst + i * kPkTile, &tmA, (int)(2 * k), (int)(i * a.a_rows + m0), pk_full + 8 * s);
+        for (int j = 0; j < a.wb; j++)
+          tma_load_2d(dst + (a.wa + j) * kPkTile, &tmB, (int)(2 * k), (int)(j * a.b_rows + n0), pk_full + 8 * s);
+        issued = k + 1;
+      }
+      if (*abort_flag) {  // let issued copies land before the CTA can exit
+        for (uint32_t k = (issued > kPkSlots ? issued - kPkSlots : 0); k < issued; k++)
+          mbar_drain(pk_full + 8 * (k % kPkSlots), (k / kPkSlots) & 1);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      bool ok = true;
+      for (uint32_t k = 0; k < a.nstages && ok; k++) {
+        const uint32_t o = k % a.no;
+        if (!mbar_wait(op_full + 8 * o, (k / a.no) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t base = smem_u32(op_ring + o * op_stage);
+        for (int i = 0; i < a.wa; i++)
+          for (int j = 0; j < a.wb; j++)
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+              const uint64_t ad = sw128_desc(base + i * kOpTile + kk * 32);
+              const uint64_t bd = sw128_desc(base + (a.wa + j) * kOpTile + kk * 32);
+              mma_f8(tmem, ad, bd, a.idesc, (k | i | j | kk) != 0);
+            }
+        mma_commit(op_empty + 8 * o);
+      }
+      mma_commit(ok ? acc_full : mma_done);
+      if (!ok) mbar_drain(mma_done, 0);  // issued MMAs finish before TMEM is freed
+    }
+  } else {
+    // ---------------- decoders, then epilogue
+    const int d = tid - 64;
+    for (uint32_t k = 0; k < a.nstages; k++) {
+      const uint32_t s = k % kPkSlots, o = k % a.no;
+      if (!mbar_wait(pk_full + 8 * s, (k / kPkSlots) & 1, abort_flag)) break;
+      if (k >= (uint32_t)a.no && !mbar_wait(op_empty + 8 * o, ((k / a.no) - 1) & 1, abort_flag)) break;
+      const uint8_t *pk = pk_ring + s * pk_stage;
+      uint8_t *op = op_ring + o * op_stage;
+      const uint64_t kbase = (uint64_t)k * 128;  // first column of this stage
+      for (int r = d; r < planes * 128; r += 32 * kDecWarps) {
+        const int t = r >> 7, row = r & 127;
+        const bool isA = t < a.wa;
+        const int pl = isA ? t : t - a.wa;
+        const bool bip = isA ? a.a_bip : a.b_bip;
+        const uint32_t code = ((isA ? a.a_code : a.b_code) >> (8 * pl)) & 0xFFu;
+        const uint4 w = *reinterpret_cast<const uint4 *>(pk + t * kPkTile + row * 16);
+        const uint32_t wv[4] = {w.x, w.y, w.z, w.w};  // columns 0-31, 32-63, 64-95, 96-127
+        uint8_t *dst = op + t * kOpTile + row * 128;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {  // 16-byte chunk c holds columns 16c .. 16c+15
+          const uint32_t bits = (wv[c >> 1] >> (16 * (c & 1))) & 0xFFFFu;
+          uint32_t q[4];
+#pragma unroll
+          for (int n = 0; n < 4; n++) {
+            const uint32_t sp = spread4((bits >> (4 * n)) & 0xFu);
+            if (bip) {
+              // +-1, except columns past the real K: their zero padding bits must stay 0, not -1
+              q[n] = (sp * 0x80u) ^ 0xB8B8B8B8u;
+              const uint64_t c0 = kbase + 16 * c + 4 * n;
+              if (c0 + 4 > a.K) q[n] &= c0 >= a.K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (a.K - c0))));
+            } else {
+              q[n] = sp * code;
+            }
+          }
+          *reinterpret_cast<uint4 *>(dst + ((c ^ (row & 7)) << 4)) = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+      }
+      // generic-proxy writes become visible to tcgen05.mma (async proxy) via fence + mbarrier release
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(op_full + 8 * o);
+      mbar_arrive(pk_empty + 8 * s);
+    }
+    // epilogue: warp w reads TMEM lanes 32*(w%4)..+31 (output rows), half of the columns
+    // warp-uniform decision: tcgen05.ld is a whole-warp instruction
+    if (__all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag))) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int quarter = warp & 3, half = (warp - 2) >> 2;
+      const uint64_t gm = m0 + quarter * 32 + lane;
+#pragma unroll 1
+      for (int cb = 0; cb < 2; cb++) {
+        const int col = half * 64 + cb * 32;
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)col;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+              "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+              "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (gm < a.M) {
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const uint64_t gn = n0 + col + j;
+            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  }
+}
+
+// Throughput probe: one CTA per SM, one thread issuing back-to-back
+// tcgen05.mma (M=128, N=256) from fixed zeroed shared tiles; kind 0 = e4m3
+// (K=32), kind 1 = bf16 (K=16).  A commit + bounded wait closes every 64 MMAs.
+__global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters, int kind) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 48 * 1024);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  for (int i = threadIdx.x; i < 48 * 1024 / 16; i += blockDim.x)
+    reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(bar), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  if (threadIdx.x == 0) {
+    const uint32_t a0 = smem_u32(smem), b0 = a0 + 16 * 1024;
+    const uint32_t idesc = (1u << 4) | (kind ? ((1u << 7) | (1u << 10)) : 0u) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+    uint32_t phase = 0;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll 1
+      for (int rep = 0; rep < 16; rep++)
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) {
+          const uint64_t ad = sw128_desc(a0 + kk * 32), bd = sw128_desc(b0 + kk * 32);
+          if (kind)
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(1u));
+          else
+            mma_f8(tmem, ad, bd, idesc, 1u);
+        }
+      mma_commit(smem_u32(bar));
+      if (!mbar_wait(smem_u32(bar), phase, abort_flag)) break;
+      phase ^= 1;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+  }
+}
+
+// e4m3 byte of +-2^e (e in [0, 7]).
+uint32_t e4m3_pow2(int e, bool neg) { return (uint32_t)(((e + 7) << 3) | (neg ? 0x80 : 0)); }
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// Tensor map over all planes of one operand: 2-D u64 [nbits * nrows_a][wpr], box 128 rows x 2 words.
+bool make_plane_map(CUtensorMap *map, const Mat &m) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {m.wpr(), m.nbits * m.nrows_a};
+  cuuint64_t strides[1] = {m.wpr() * 8};
+  cuuint32_t box[2] = {2, 128};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, m.planes, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+uint64_t max_abs(const Mat &m) {
+  if (m.bipolar()) return 1;
+  return m.issigned ? (1ull << (m.nbits - 1)) : ((1ull << m.nbits) - 1);
+}
+
+constexpr size_t kSmemCap = 225 * 1024;
+
+size_t tc_smem(int planes, int no) {
+  return 1024 + (size_t)no * planes * kOpTile + (size_t)kPkSlots * planes * kPkTile + 8 * (2 * kPkSlots + 2 * no + 2) +
+         16;
+}
+
+}  // namespace
+
+// The tensor-core pipe applies when every partial sum stays exact in fp32,
+// at most 4 planes per operand and 5 in total fit the operand ring, and
+// both dimensions fill at least half a tile.
+bool tc_supported(const gbs_ctx *c) {
+  const Mat &A = c->lhs, &B = c->rhs;
+  if (A.nbits > 4 || B.nbits > 4 || A.nbits + B.nbits > 5) return false;
+  if (A.nrows < 64 || B.nrows < 64 || A.ncols == 0) return false;
+  if ((double)A.ncols * (double)max_abs(A) * (double)max_abs(B) >= 16777216.0) return false;
+  if (A.nrows_a * A.nbits > (1ull << 31) || B.nrows_a * B.nbits > (1ull << 31)) return false;
+  return encode_fn() != nullptr;
+}
+
+cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s) {
+  if (!c->tc_maps_ready) {
+    if (!make_plane_map(reinterpret_cast<CUtensorMap *>(c->tc_map_a), c->lhs) ||
+        !make_plane_map(reinterpret_cast<CUtensorMap *>(c->tc_map_b), c->rhs))
+      return cudaErrorInvalidValue;
+    c->tc_maps_ready = true;
+  }
+  const Mat &A = c->lhs, &B = c->rhs;
+  TcArgs a;
+  memset(&a, 0, sizeof(a));
+  a.C = c->res;
+  a.M = A.nrows;
+  a.N = B.nrows;
+  a.K = A.ncols;
+  a.nstages = (uint32_t)(A.wpr() / 2);
+  a.a_rows = (uint32_t)A.nrows_a;
+  a.b_rows = (uint32_t)B.nrows_a;
+  a.wa = (int)A.nbits;
+  a.wb = (int)B.nbits;
+  a.a_bip = A.bipolar();
+  a.b_bip = B.bipolar();
+  for (int i = 0; i < a.wa; i++)
+    a.a_code |= e4m3_pow2(i, A.issigned && !A.bipolar() && i == a.wa - 1) << (8 * i);
+  for (int j = 0; j < a.wb; j++)
+    a.b_code |= e4m3_pow2(j, B.issigned && !B.bipolar() && j == a.wb - 1) << (8 * j);
+  // kind::f8f6f4: D fp32, A and B e4m3, both K-major, N = 128, M = 128
+  a.idesc = (1u << 4) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+  const int planes = a.wa + a.wb;
+  int no = 4;
+  while (no > 1 && tc_smem(planes, no) > kSmemCap) no--;
+  a.no = no;
+  const size_t smem = tc_smem(planes, no);
+  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + kBN - 1) / kBN));
+  gemm_tc_kernel<<<grid, kThreads, smem, s>>>(*reinterpret_cast<const CUtensorMap *>(c->tc_map_a),
+                                               *reinterpret_cast<const CUtensorMap *>(c->tc_map_b), a);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// Sustained tcgen05 MMA rate in FLOP/s (2 per multiply-add) for e4m3 and bf16.
+int tc_peaks(double *f8, double *bf16) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = 1024 + 48 * 1024 + 64;
+  cudaError_t e = cudaFuncSetAttribute(peak_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_tc_peaks");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double out[2] = {0, 0};
+  const int iters = 200;
+  for (int kind = 0; kind < 2; kind++) {
+    peak_tc_kernel<<<sms, 128, smem>>>(4, kind);
+    cudaDeviceSynchronize();
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+      cudaEventRecord(e0);
+      peak_tc_kernel<<<sms, 128, smem>>>(iters, kind);
+      cudaEventRecord(e1);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) best = ms;
+    }
+    const double k = kind ? 16.0 : 32.0;
+    out[kind] = 2.0 * sms * (double)iters * 64.0 * 128.0 * 256.0 * k / (best * 1e-3);
+  }
+  count_launch(8);
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_tc_peaks");
+  if (f8) *f8 = out[0];
+  if (bf16) *bf16 = out[1];
+  return GBS_OK;
+}
+
+uint32_t tc_error_word() {
+  uint32_t v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(v)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0xFFFFFFFFu;
+  }
+  return v;
+}
+
+}  // namespace gbs

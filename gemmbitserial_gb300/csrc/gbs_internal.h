@@ -95,6 +95,10 @@ struct gbs_ctx {
   size_t stage_bytes = 0;
   int device = 0;
   int pipe = GBS_PIPE_AUTO;
+  // TMA descriptors (CUtensorMap, 128 bytes, 64-byte aligned) over the planes, built on first use
+  alignas(64) unsigned char tc_map_a[128];
+  alignas(64) unsigned char tc_map_b[128];
+  bool tc_maps_ready = false;
 };
 
 namespace gbs {
@@ -126,5 +130,10 @@ cudaError_t launch_pack_grouped(const PackJob *jobs, int njobs, uint64_t total_w
 cudaError_t launch_rowsum_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s);
 cudaError_t launch_gemm_bmma(const GemmShape &g, const Epilogue &e, cudaStream_t s);
 bool bmma_supported(int wa, int wb, int use_xor);
+bool tc_supported(const gbs_ctx *c);
+cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s);
+uint32_t tc_error_word();
+int tc_peaks(double *f8, double *bf16);
+int effective_pipe(const gbs_ctx *c);
 
 }  // namespace gbs

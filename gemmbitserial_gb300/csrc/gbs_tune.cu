@@ -82,11 +82,13 @@ __global__ void __launch_bounds__(256) peak_fma(const float *in, float *out, int
 
 }  // namespace
 
-int choose_pipe(const gbs_ctx *) {
-  // On GB300 the CUDA-core pipe sustains about twice the b1 tensor pipe's
-  // AND+popcount rate (gbs_pipe_peaks), for every shape class.
-  return GBS_PIPE_POPC;
-}
+// Measured on GB300: the CUDA-core POPC pipe sustains ~160 T bit-op/s and the
+// b1 mma.sync pipe about half that (gbs_pipe_peaks), while tcgen05 e4m3
+// multiply-adds run at ~1.75 P/s (gbs_tc_peaks).  So every shape the
+// tensor-core pipe covers exactly goes there; the rest (8-bit widths, more
+// than 5 planes, K beyond the fp32-exact bound, skinny shapes) use the CUDA
+// cores.  The b1 pipe is never the better choice on this GPU.
+int choose_pipe(const gbs_ctx *c) { return tc_supported(c) ? GBS_PIPE_TC : GBS_PIPE_POPC; }
 
 }  // namespace gbs
 

@@ -58,7 +58,8 @@ enum { GBS_LHS = 0, GBS_RHS = 1 };
 enum {
   GBS_PIPE_AUTO = 0, /* per-shape choice (tuner store, else built-in rule) */
   GBS_PIPE_POPC = 1, /* CUDA cores: LOP3 AND/XOR + POPC */
-  GBS_PIPE_BMMA = 2  /* tensor pipe: mma.sync b1 AND/XOR + popc */
+  GBS_PIPE_BMMA = 2, /* tensor pipe: mma.sync b1 AND/XOR + popc */
+  GBS_PIPE_TC = 3    /* 5th-gen tensor cores: tcgen05.mma on plane pairs as fp8 {0, +-2^i} */
 };
 
 typedef struct gbs_ctx gbs_ctx; /* opaque; copies of the handle alias one context */
@@ -219,6 +220,11 @@ GBS_API int gbs_group_free(gbs_group *g);
  * No reference counterpart: the reference has a single CPU pipe. */
 GBS_API int gbs_pipe_peaks(double *popc_bitops, double *bmma_bitops);
 
+/* Measures the sustained tcgen05.mma rate (FLOP/s, 2 per multiply-add) of the
+ * current device for e4m3 (kind::f8f6f4) and bf16 (kind::f16) operands with
+ * an fp32 accumulator, M=128 N=256 (~10 ms).  No reference counterpart. */
+GBS_API int gbs_tc_peaks(double *f8_flops, double *bf16_flops);
+
 /* Measures the sustained FP32 FMA rate (FLOP/s, 2 per FMA) of the current
  * device, the roofline of gbs_adjoint (~20 ms).  No reference counterpart. */
 GBS_API int gbs_fma_peak(double *flops);
@@ -233,6 +239,9 @@ GBS_API const char *gbs_version(void);
 
 /* Makes the n-th next allocation made by the library fail (n >= 1); 0 disarms. */
 GBS_API void gbs_debug_fail_alloc_after(int n);
+
+/* Error bits raised by tensor-core kernels whose bounded waits gave up (0 = none). */
+GBS_API uint32_t gbs_debug_tc_error(void);
 
 /* Overwrites tile `tile` of a group's queue with an invalid descriptor, to
  * exercise the grouped kernel's descriptor validation (host-side injection). */

@@ -1,0 +1,114 @@
+"""The 5th-generation tensor-core pipe (tcgen05.mma on plane pairs as fp8
+{0, +-2^i} operands, TMEM accumulation): bit-exact against the oracle and
+the reference's own full-size results, including sums up to just below 2^24
+(the exactness bound the pipe is selected under)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gemmbitserial_gb300 import _capi, datagen
+from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext, gemmBitSerial
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CFG = json.load(open(os.path.join(GOLD, "ref_configs.json")))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib(gbs_lib):
+    import torch
+    assert torch.cuda.is_available()
+    return gbs_lib
+
+
+def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True):
+    M, K = A.shape
+    N = B.shape[0]
+    ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    try:
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        if expect_tc:
+            assert ctx.pipe == _capi.GBS_PIPE_TC, "tensor-core pipe not applicable"
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        gemmBitSerial(ctx)
+        return ctx.res.reshape(N, M)
+    finally:
+        deallocGEMMContext(ctx)
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_tc_small_first():
+    A = datagen.operand(datagen.SEED_BASE + 500, 128, 256, 1, "u")
+    B = datagen.operand(datagen.SEED_BASE + 501, 128, 256, 1, "u")
+    got = tc_gemm(A, B, 1, 1, False, False)
+    assert _capi.load().gbs_debug_tc_error() == 0
+    assert np.array_equal(got, O.oracle_gemm(A, B, 1, 1, False, False))
+
+
+ENCS = [(1, "u"), (1, "b"), (2, "u"), (2, "s"), (3, "u"), (3, "s"), (4, "u"), (4, "s")]
+
+
+@pytest.mark.parametrize("shape", [(128, 256, 128), (200, 1000, 333), (64, 128, 64), (300, 3000, 129),
+                                   (129, 64, 700)])
+def test_tc_encodings_vs_oracle(shape):
+    M, K, N = shape
+    rng = np.random.default_rng(M + K + N)
+    for (wa, ea) in ENCS:
+        for (wb, eb) in ENCS:
+            if wa + wb > 5:
+                continue
+            A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+            B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+            sa, sb = ea != "u", eb != "u"
+            assert np.array_equal(tc_gemm(A, B, wa, wb, sa, sb), O.oracle_gemm(A, B, wa, wb, sa, sb)), \
+                (shape, wa, ea, wb, eb)
+    assert _capi.load().gbs_debug_tc_error() == 0
+
+
+@pytest.mark.parametrize("name", sorted(CFG))
+def test_tc_full_size_workloads(name):
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+    assert sha(tc_gemm(A, B, wA, wB, sA, sB, expect_tc=min(M, N) >= 64)) == CFG[name]["sha256"]
+
+
+def test_tc_sums_near_the_exactness_bound():
+    """4-bit x 1-bit unsigned, every product 15: sums of 15 * K with K = 1,118,464 - 64 stay < 2^24."""
+    M, N = 128, 128
+    K = (1 << 24) // 15 - 64
+    A = np.full((M, K), 15, np.int8)
+    B = np.ones((N, K), np.int8)
+    B[1::2, ::3] = 0
+    got = tc_gemm(A, B, 4, 1, False, False)
+    want = O.oracle_gemm(A, B, 4, 1, False, False, threads=16)
+    assert np.array_equal(got, want)
+    # signed: alternating +-8 * 1 partial sums swing across zero
+    A2 = np.where((np.arange(K) // 7) % 2 == 0, -8, 7).astype(np.int8)[None, :].repeat(M, 0)
+    got2 = tc_gemm(A2, B, 4, 1, True, False)
+    assert np.array_equal(got2, O.oracle_gemm(A2, B, 4, 1, True, False, threads=16))
+    assert _capi.load().gbs_debug_tc_error() == 0
+
+
+def test_tc_pipe_declines_what_it_cannot_do_exactly():
+    """8-bit operands or K beyond the fp32 bound fall back to the CUDA-core pipe."""
+    for (M, K, N, wa, wb) in [(128, 256, 128, 8, 1), (128, 1 << 21, 128, 4, 1), (16, 256, 128, 1, 1)]:
+        ctx = allocGEMMContext(M, K, N, wa, wb, False, False)
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        assert ctx.pipe == _capi.GBS_PIPE_POPC
+        deallocGEMMContext(ctx)
+
+
+def test_tc_peaks_probe():
+    import ctypes as C
+    f8, bf = C.c_double(), C.c_double()
+    _capi.check(_capi.load().gbs_tc_peaks(C.byref(f8), C.byref(bf)))
+    print(f"tcgen05 e4m3 {f8.value / 1e12:.0f} TFLOP/s, bf16 {bf.value / 1e12:.0f} TFLOP/s")
+    assert f8.value > 1e14 and bf.value > 1e14
+    assert _capi.load().gbs_debug_tc_error() == 0
