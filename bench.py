@@ -438,17 +438,20 @@ def run_ours(args):
         return
     # ---- roofline of the forward kernel against the measured peak of the pipe it ran on
     kpad = (K + 63) // 64 * 64
-    if pipe == _capi.GBS_PIPE_TC:
+    if pipe in (_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS):
         f8, bf16 = C.c_double(), C.c_double()
         _capi.check(lib.gbs_tc_peaks(C.byref(f8), C.byref(bf16)))
         kernel = "gemm_tc_kernel"
-        work = 2.0 * M * N * K * wA * wB  # fp8 plane-pair multiply-adds on the tensor pipe
+        digits = pipe == _capi.GBS_PIPE_TC
+        # fp8 multiply-adds the tensor pipe must do: one per (m, n, k) in digit mode, one per plane pair otherwise
+        work = 2.0 * M * N * K * (1 if digits else wA * wB)
         achieved = work / (ms * 1e-3) / 1e12
         peak = f8.value / 1e12
         roof = {"bound": "tensor", "kernel": kernel, "achieved": round(achieved, 2), "peak": round(peak, 2),
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
                 "peak_source": "measured in-process (gbs_tc_peaks: tcgen05.mma kind::f8f6f4, M=128 N=256)",
-                "work": "2*M*N*K*wA*wB fp8 plane-pair FLOPs",
+                "work": "2*M*N*K fp8 FLOPs (digit mode: all plane pairs in one MMA)" if digits
+                        else "2*M*N*K*wA*wB fp8 plane-pair FLOPs",
                 "bf16_peak_measured": round(bf16.value / 1e12, 1)}
     else:
         popc, bmma = C.c_double(), C.c_double()
@@ -479,7 +482,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded splitmix64)",
             "config": dict(desc, parallelism=f"replicas x{world}", l2="flushed before every step (256 MiB write, outside the timed events)",
-                           pipe={1: "popc", 2: "bmma", 3: "tcgen05"}.get(pipe, str(pipe))),
+                           pipe={1: "popc", 2: "bmma", 3: "tcgen05-digits", 4: "tcgen05-pairs"}.get(pipe, str(pipe))),
             "parity": parity,
             "e2e": {"value": round(gops(M, K, N, e2e_s) * world, 3), "unit": "GOPS",
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),

@@ -120,7 +120,7 @@ int choose_pipe(const gbs_ctx *c);
 // the CUDA cores for shapes it does not cover.
 int effective_pipe(const gbs_ctx *c) {
   const int p = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
-  if (p == GBS_PIPE_TC && !tc_supported(c)) return GBS_PIPE_POPC;
+  if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS) && !tc_supported(c)) return GBS_PIPE_POPC;
   return p;
 }
 
@@ -271,7 +271,7 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
 
 int gbs_set_pipe(gbs_ctx *c, int pipe) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_pipe: ctx is NULL");
-  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_TC) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
+  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_TC_PAIRS) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
   c->pipe = pipe;
   return GBS_OK;
 }
@@ -308,8 +308,8 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.wb = (int)c->rhs.nbits;
   const int pipe = effective_pipe(c);
   cudaError_t ke;
-  if (pipe == GBS_PIPE_TC) {
-    ke = launch_gemm_tc(c, s);
+  if (pipe == GBS_PIPE_TC || pipe == GBS_PIPE_TC_PAIRS) {
+    ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC);
   } else if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
     if (e.use_xor) {
       // ncols - 2*popc(a^b) = 4*popc(a&b) - rsA - rsB - ncols, rs = bipolar row sums (2*popc - ncols)

@@ -38,24 +38,35 @@ static __device__ uint32_t g_tc_error;
 
 namespace {
 
-constexpr int kBM = 128, kBN = 128;
-constexpr int kOpTile = 128 * 128;  // bytes of one plane's operand tile (128 rows x 128 e4m3)
-constexpr int kPkTile = 128 * 16;   // bytes of one plane's packed stage (128 rows x 128 bits)
-constexpr int kDecWarps = 8;
+constexpr int kBM = 128;
+constexpr int kRowB = 128;          // bytes per operand row per stage (128 e4m3 values of K)
+constexpr int kPkRowB = 16;         // packed bytes per row per plane per stage (128 bits)
+constexpr int kDecWarps = 12;  // warps 2..13 decode; warps 2..9 also run the epilogue
 constexpr int kThreads = 64 + 32 * kDecWarps;
 constexpr int kPkSlots = 4;
 constexpr uint32_t kWaitLimit = 1u << 20;
+
+// How the planes of one operand become e4m3 operand tiles.  DIGIT mode: one
+// tile whose value is the whole few-bit number (all planes at once, so one
+// MMA covers every plane pair).  PAIR mode: one tile per plane holding
+// {0, +-2^i}.  A tile's value for a given code (its planes' bits, plane
+// first+b as bit b) is tab byte [code]: 16 entries, 4 per word.
+struct TcOperand {
+  int ntiles;
+  int first[4], count[4];
+  uint32_t tab[4][4];
+  int bip;  // bipolar operand: columns past K must decode to 0, not -1
+};
 
 struct TcArgs {
   int32_t *C;
   uint64_t M, N, K;
   uint32_t nstages;         // K stages of 128 bits
   uint32_t a_rows, b_rows;  // padded rows per plane (TMA row coordinate of plane i = i * rows + tile row)
-  int wa, wb, a_bip, b_bip, no;
-  uint32_t a_code, b_code;  // packed e4m3 codes of a set bit, one byte per plane (planes 0..3)
+  int wa, wb, no;
   uint32_t idesc;
+  TcOperand A, B;
 };
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
@@ -122,13 +133,42 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
 // bits at 0..3, 7..10, 14..17, 21..24 without carries, the mask keeps 0, 8, 16, 24.
 __device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
 
+__device__ __forceinline__ uint32_t bfe4(uint32_t x, int sh) {
+  uint32_t r;
+  asm("bfe.u32 %0, %1, %2, 4;" : "=r"(r) : "r"(x), "r"(sh));
+  return r;
+}
+
+// e4m3 bytes of 4 consecutive columns of one tile row: codes from the tile's
+// planes (bits at column offset `sh` of each plane's 32-bit word), then a
+// byte-permute lookup in the tile's 16-entry table.  Plane p's nibble is
+// spread straight to bit p of each byte (multiplier and mask shifted by p).
+template <int CNT>
+__device__ __forceinline__ uint32_t decode4(const uint32_t (&pw)[4], int sh, const uint32_t (&tab)[4]) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int p = 0; p < CNT; p++) c |= (bfe4(pw[p], sh) * (0x00204081u << p)) & (0x01010101u << p);
+  if (CNT == 1) return c;  // caller maps 0/1 bytes itself
+  const uint32_t t = c | (c >> 4);                        // byte 0 = c0 | c1<<4, byte 2 = c2 | c3<<4
+  const uint32_t sel = __byte_perm(t, 0u, 0x0020u);        // nibbles c0 c1 c2 c3 in the low 16 bits
+  if (CNT <= 3) return __byte_perm(tab[0], tab[1], sel);
+  const uint32_t lo = __byte_perm(tab[0], tab[1], sel & 0x7777u);
+  const uint32_t hi = __byte_perm(tab[2], tab[3], sel & 0x7777u);
+  const uint32_t m = ((c >> 3) & 0x01010101u) * 0xFFu;     // codes 8..15 take the high table
+  return (lo & ~m) | (hi & m);
+}
+
+template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int planes = a.wa + a.wb;
-  const uint32_t op_stage = planes * kOpTile, pk_stage = planes * kPkTile;
+  const int ntA = a.A.ntiles, ntB = a.B.ntiles;
+  const uint32_t a_tile = kBM * kRowB, b_tile = BN * kRowB;
+  const uint32_t op_stage = ntA * a_tile + ntB * b_tile;
+  const uint32_t pk_a = kBM * kPkRowB, pk_b = BN * kPkRowB;  // packed bytes of one plane per stage
+  const uint32_t pk_stage = a.wa * pk_a + a.wb * pk_b;
   uint8_t *op_ring = smem;
   uint8_t *pk_ring = op_ring + a.no * op_stage;
   uint64_t *bars = reinterpret_cast<uint64_t *>(pk_ring + kPkSlots * pk_stage);
@@ -138,16 +178,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t acc_full = op_empty + 8 * a.no, mma_done = acc_full + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kPkSlots + 2 * a.no + 2);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-  const uint64_t m0 = (uint64_t)blockIdx.x * kBM, n0 = (uint64_t)blockIdx.y * kBN;
+  const uint64_t m0 = (uint64_t)blockIdx.x * kBM, n0 = (uint64_t)blockIdx.y * BN;
 
   if (tid == 0) {
     for (int i = 0; i < kPkSlots; i++) {
-      mbar_init(pk_full + 8 * i, 1);                   // producer's expect_tx + TMA bytes
-      mbar_init(pk_empty + 8 * i, 32 * kDecWarps);     // every decoder thread has read the slot
+      mbar_init(pk_full + 8 * i, 1);                // producer's expect_tx + TMA bytes
+      mbar_init(pk_empty + 8 * i, 32 * kDecWarps);  // every decoder thread has read the slot
     }
     for (int i = 0; i < a.no; i++) {
-      mbar_init(op_full + 8 * i, 32 * kDecWarps);      // every decoder thread has written its rows
-      mbar_init(op_empty + 8 * i, 1);                  // tcgen05.commit of the MMAs that read the slot
+      mbar_init(op_full + 8 * i, 32 * kDecWarps);   // every decoder thread has written its chunks
+      mbar_init(op_empty + 8 * i, 1);               // tcgen05.commit of the MMAs that read the slot
     }
     mbar_init(acc_full, 1);
     mbar_init(mma_done, 1);
@@ -155,7 +195,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "n"(BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -164,7 +205,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    // ---------------- TMA producer
+    // ---------------- TMA producer: 128-row boxes (two per rhs plane when BN = 256)
     if (lane == 0) {
       uint32_t issued = 0;
       for (uint32_t k = 0; k < a.nstages; k++) {
@@ -173,9 +214,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_expect_tx(pk_full + 8 * s, pk_stage);
         const uint32_t dst = smem_u32(pk_ring + s * pk_stage);
         for (int i = 0; i < a.wa; i++)
-          tma_load_2d(dst + i * kPkTile, &tmA, (int)(2 * k), (int)(i * a.a_rows + m0), pk_full + 8 * s);
+          tma_load_2d(dst + i * pk_a, &tmA, (int)(2 * k), (int)(i * a.a_rows + m0), pk_full + 8 * s);
         for (int j = 0; j < a.wb; j++)
-          tma_load_2d(dst + (a.wa + j) * kPkTile, &tmB, (int)(2 * k), (int)(j * a.b_rows + n0), pk_full + 8 * s);
+          for (int h = 0; h < BN / 128; h++)
+            tma_load_2d(dst + a.wa * pk_a + j * pk_b + h * 128 * kPkRowB, &tmB, (int)(2 * k),
+                        (int)(j * a.b_rows + n0 + 128 * h), pk_full + 8 * s);
         issued = k + 1;
       }
       if (*abort_flag) {  // let issued copies land before the CTA can exit
@@ -184,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer
+    // ---------------- MMA issuer: every (lhs tile, rhs tile) pair, 4 K steps of 32
     if (lane == 0) {
       bool ok = true;
       for (uint32_t k = 0; k < a.nstages && ok; k++) {
@@ -195,12 +238,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t base = smem_u32(op_ring + o * op_stage);
-        for (int i = 0; i < a.wa; i++)
-          for (int j = 0; j < a.wb; j++)
+        for (int i = 0; i < ntA; i++)
+          for (int j = 0; j < ntB; j++)
 #pragma unroll
             for (int kk = 0; kk < 4; kk++) {
-              const uint64_t ad = sw128_desc(base + i * kOpTile + kk * 32);
-              const uint64_t bd = sw128_desc(base + (a.wa + j) * kOpTile + kk * 32);
+              const uint64_t ad = sw128_desc(base + i * a_tile + kk * 32);
+              const uint64_t bd = sw128_desc(base + ntA * a_tile + j * b_tile + kk * 32);
               mma_f8(tmem, ad, bd, a.idesc, (k | i | j | kk) != 0);
             }
         mma_commit(op_empty + 8 * o);
@@ -209,8 +252,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!ok) mbar_drain(mma_done, 0);  // issued MMAs finish before TMEM is freed
     }
   } else {
-    // ---------------- decoders, then epilogue
+    // ---------------- decoders: one task = one 16-column chunk of one tile row, then epilogue
     const int d = tid - 64;
+    const int rowsA = ntA * kBM, rows = rowsA + ntB * BN;
     for (uint32_t k = 0; k < a.nstages; k++) {
       const uint32_t s = k % kPkSlots, o = k % a.no;
       if (!mbar_wait(pk_full + 8 * s, (k / kPkSlots) & 1, abort_flag)) break;
@@ -218,48 +262,68 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint8_t *pk = pk_ring + s * pk_stage;
       uint8_t *op = op_ring + o * op_stage;
       const uint64_t kbase = (uint64_t)k * 128;  // first column of this stage
-      for (int r = d; r < planes * 128; r += 32 * kDecWarps) {
-        const int t = r >> 7, row = r & 127;
-        const bool isA = t < a.wa;
-        const int pl = isA ? t : t - a.wa;
-        const bool bip = isA ? a.a_bip : a.b_bip;
-        const uint32_t code = ((isA ? a.a_code : a.b_code) >> (8 * pl)) & 0xFFu;
-        const uint4 w = *reinterpret_cast<const uint4 *>(pk + t * kPkTile + row * 16);
-        const uint32_t wv[4] = {w.x, w.y, w.z, w.w};  // columns 0-31, 32-63, 64-95, 96-127
-        uint8_t *dst = op + t * kOpTile + row * 128;
+      for (int task = d; task < rows * 8; task += 32 * kDecWarps) {
+        const int r = task >> 3, c = task & 7;
+        const bool isA = r < rowsA;
+        const int rr = isA ? r : r - rowsA;
+        const int t = isA ? rr / kBM : rr / BN, row = isA ? rr % kBM : rr % BN;
+        const TcOperand &P = isA ? a.A : a.B;
+        const int cnt = P.count[t];
+        uint32_t pw[4];
 #pragma unroll
-        for (int c = 0; c < 8; c++) {  // 16-byte chunk c holds columns 16c .. 16c+15
-          const uint32_t bits = (wv[c >> 1] >> (16 * (c & 1))) & 0xFFFFu;
-          uint32_t q[4];
+        for (int p = 0; p < 4; p++) {
+          pw[p] = 0u;
+          if (p < cnt) {
+            const int plane = P.first[t] + p;
+            const uint8_t *src = isA ? pk + plane * pk_a : pk + a.wa * pk_a + plane * pk_b;
+            pw[p] = *reinterpret_cast<const uint32_t *>(src + row * kPkRowB + (c >> 1) * 4);
+          }
+        }
+        uint32_t tab[4] = {P.tab[t][0], P.tab[t][1], P.tab[t][2], P.tab[t][3]};
+        uint32_t q[4];
+        const int sh0 = 16 * (c & 1);
+        if (cnt == 1) {
+          // one plane: bytes are 0/1, mapped with two table bytes (bipolar: -1/+1)
+          const uint32_t v0 = tab[0] & 0xFFu, v1 = (tab[0] >> 8) & 0xFFu;
 #pragma unroll
           for (int n = 0; n < 4; n++) {
-            const uint32_t sp = spread4((bits >> (4 * n)) & 0xFu);
-            if (bip) {
-              // +-1, except columns past the real K: their zero padding bits must stay 0, not -1
-              q[n] = (sp * 0x80u) ^ 0xB8B8B8B8u;
-              const uint64_t c0 = kbase + 16 * c + 4 * n;
-              if (c0 + 4 > a.K) q[n] &= c0 >= a.K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (a.K - c0))));
-            } else {
-              q[n] = sp * code;
-            }
+            const uint32_t sp = decode4<1>(pw, sh0 + 4 * n, tab);
+            q[n] = sp * v1 + (sp ^ 0x01010101u) * v0;
           }
-          *reinterpret_cast<uint4 *>(dst + ((c ^ (row & 7)) << 4)) = make_uint4(q[0], q[1], q[2], q[3]);
+        } else if (cnt == 2) {
+#pragma unroll
+          for (int n = 0; n < 4; n++) q[n] = decode4<2>(pw, sh0 + 4 * n, tab);
+        } else if (cnt == 3) {
+#pragma unroll
+          for (int n = 0; n < 4; n++) q[n] = decode4<3>(pw, sh0 + 4 * n, tab);
+        } else {
+#pragma unroll
+          for (int n = 0; n < 4; n++) q[n] = decode4<4>(pw, sh0 + 4 * n, tab);
         }
+        if (P.bip) {  // bipolar zero-padding columns past K stay 0 instead of -1
+#pragma unroll
+          for (int n = 0; n < 4; n++) {
+            const uint64_t c0 = kbase + 16 * c + 4 * n;
+            if (c0 + 4 > a.K) q[n] &= c0 >= a.K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (a.K - c0))));
+          }
+        }
+        uint8_t *dst = op + (isA ? t * a_tile : ntA * a_tile + t * b_tile) + row * kRowB;
+        *reinterpret_cast<uint4 *>(dst + ((c ^ (row & 7)) << 4)) = make_uint4(q[0], q[1], q[2], q[3]);
       }
       // generic-proxy writes become visible to tcgen05.mma (async proxy) via fence + mbarrier release
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(op_full + 8 * o);
       mbar_arrive(pk_empty + 8 * s);
     }
-    // epilogue: warp w reads TMEM lanes 32*(w%4)..+31 (output rows), half of the columns
-    // warp-uniform decision: tcgen05.ld is a whole-warp instruction
-    if (__all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag))) {
+    // epilogue (warps 2..9): warp w reads TMEM lanes 32*(w%4)..+31 (output rows), half of
+    // the columns.  The decision is warp-uniform because tcgen05.ld is a whole-warp instruction.
+    if (warp < 10 && __all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag))) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int quarter = warp & 3, half = (warp - 2) >> 2;
       const uint64_t gm = m0 + quarter * 32 + lane;
 #pragma unroll 1
-      for (int cb = 0; cb < 2; cb++) {
-        const int col = half * 64 + cb * 32;
+      for (int cb = 0; cb < BN / 64; cb++) {
+        const int col = half * (BN / 2) + cb * 32;
         uint32_t v[32];
         const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)col;
         asm volatile(
@@ -286,7 +350,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(BN));
   }
 }
 
@@ -346,8 +410,42 @@ __global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters, int kind) {
   }
 }
 
-// e4m3 byte of +-2^e (e in [0, 7]).
-uint32_t e4m3_pow2(int e, bool neg) { return (uint32_t)(((e + 7) << 3) | (neg ? 0x80 : 0)); }
+// e4m3 byte of a small integer (|v| <= 16 is exact: 3 mantissa bits below 2^4).
+uint32_t e4m3_int(int v) {
+  if (v == 0) return 0u;
+  const uint32_t sign = v < 0 ? 0x80u : 0u;
+  int m = v < 0 ? -v : v, e = 0;
+  while ((m >> (e + 1)) != 0) e++;
+  const int frac = (m - (1 << e)) << (3 - e);  // exact for e <= 3, zero for m = 16
+  return sign | (uint32_t)((e + 7) << 3) | (uint32_t)(e <= 3 ? frac : 0);
+}
+
+// Value of code `code` (bit b = plane first+b) for planes [first, first+count) of operand m.
+int code_value(const Mat &m, int first, int count, int code) {
+  if (m.bipolar()) return (code & 1) ? 1 : -1;
+  int v = 0;
+  for (int b = 0; b < count; b++)
+    if ((code >> b) & 1) {
+      const int plane = first + b;
+      const int w = 1 << plane;
+      v += (m.issigned && plane == (int)m.nbits - 1) ? -w : w;
+    }
+  return v;
+}
+
+TcOperand make_operand(const Mat &m, bool digits) {
+  TcOperand op;
+  memset(&op, 0, sizeof(op));
+  op.bip = m.bipolar() ? 1 : 0;
+  op.ntiles = digits ? 1 : (int)m.nbits;
+  for (int t = 0; t < op.ntiles; t++) {
+    op.first[t] = digits ? 0 : t;
+    op.count[t] = digits ? (int)m.nbits : 1;
+    for (int code = 0; code < (1 << op.count[t]); code++)
+      op.tab[t][code >> 2] |= e4m3_int(code_value(m, op.first[t], op.count[t], code)) << (8 * (code & 3));
+  }
+  return op;
+}
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -387,9 +485,10 @@ uint64_t max_abs(const Mat &m) {
 
 constexpr size_t kSmemCap = 225 * 1024;
 
-size_t tc_smem(int planes, int no) {
-  return 1024 + (size_t)no * planes * kOpTile + (size_t)kPkSlots * planes * kPkTile + 8 * (2 * kPkSlots + 2 * no + 2) +
-         16;
+size_t tc_smem(int ntA, int ntB, int wa, int wb, int bn, int no) {
+  const size_t op_stage = (size_t)ntA * kBM * kRowB + (size_t)ntB * bn * kRowB;
+  const size_t pk_stage = (size_t)wa * kBM * kPkRowB + (size_t)wb * bn * kPkRowB;
+  return 1024 + no * op_stage + kPkSlots * pk_stage + 8 * (2 * kPkSlots + 2 * no + 2) + 16;
 }
 
 }  // namespace
@@ -406,7 +505,7 @@ bool tc_supported(const gbs_ctx *c) {
   return encode_fn() != nullptr;
 }
 
-cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s) {
+cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits) {
   if (!c->tc_maps_ready) {
     if (!make_plane_map(reinterpret_cast<CUtensorMap *>(c->tc_map_a), c->lhs) ||
         !make_plane_map(reinterpret_cast<CUtensorMap *>(c->tc_map_b), c->rhs))
@@ -425,24 +524,30 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s) {
   a.b_rows = (uint32_t)B.nrows_a;
   a.wa = (int)A.nbits;
   a.wb = (int)B.nbits;
-  a.a_bip = A.bipolar();
-  a.b_bip = B.bipolar();
-  for (int i = 0; i < a.wa; i++)
-    a.a_code |= e4m3_pow2(i, A.issigned && !A.bipolar() && i == a.wa - 1) << (8 * i);
-  for (int j = 0; j < a.wb; j++)
-    a.b_code |= e4m3_pow2(j, B.issigned && !B.bipolar() && j == a.wb - 1) << (8 * j);
-  // kind::f8f6f4: D fp32, A and B e4m3, both K-major, N = 128, M = 128
-  a.idesc = (1u << 4) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
-  const int planes = a.wa + a.wb;
+  a.A = make_operand(A, digits);
+  a.B = make_operand(B, digits);
+  const int bn = (digits && a.N > 128) ? 256 : 128;
+  // kind::f8f6f4: D fp32, A and B e4m3, both K-major, M = 128, N = bn
+  a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
   int no = 4;
-  while (no > 1 && tc_smem(planes, no) > kSmemCap) no--;
+  while (no > 1 && tc_smem(a.A.ntiles, a.B.ntiles, a.wa, a.wb, bn, no) > kSmemCap) no--;
   a.no = no;
-  const size_t smem = tc_smem(planes, no);
-  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + kBN - 1) / kBN));
-  gemm_tc_kernel<<<grid, kThreads, smem, s>>>(*reinterpret_cast<const CUtensorMap *>(c->tc_map_a),
-                                               *reinterpret_cast<const CUtensorMap *>(c->tc_map_b), a);
+  const size_t smem = tc_smem(a.A.ntiles, a.B.ntiles, a.wa, a.wb, bn, no);
+  if (smem > kSmemCap) return cudaErrorInvalidConfiguration;
+  const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_a);
+  const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_b);
+  cudaError_t e;
+  if (bn == 256) {
+    e = cudaFuncSetAttribute(gemm_tc_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + 255) / 256));
+    gemm_tc_kernel<256><<<grid, kThreads, smem, s>>>(ma, mb, a);
+  } else {
+    e = cudaFuncSetAttribute(gemm_tc_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + 127) / 128));
+    gemm_tc_kernel<128><<<grid, kThreads, smem, s>>>(ma, mb, a);
+  }
   count_launch();
   return cudaGetLastError();
 }

@@ -131,7 +131,7 @@ cudaError_t launch_rowsum_grouped(const PackJob *jobs, int njobs, uint64_t total
 cudaError_t launch_gemm_bmma(const GemmShape &g, const Epilogue &e, cudaStream_t s);
 bool bmma_supported(int wa, int wb, int use_xor);
 bool tc_supported(const gbs_ctx *c);
-cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s);
+cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits);
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 int effective_pipe(const gbs_ctx *c);

@@ -25,14 +25,14 @@ def lib(gbs_lib):
     return gbs_lib
 
 
-def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True):
+def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True, pipe=_capi.GBS_PIPE_TC):
     M, K = A.shape
     N = B.shape[0]
     ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
     try:
-        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.set_pipe(pipe)
         if expect_tc:
-            assert ctx.pipe == _capi.GBS_PIPE_TC, "tensor-core pipe not applicable"
+            assert ctx.pipe == pipe, "tensor-core pipe not applicable"
         ctx.lhs.importRegular(A)
         ctx.rhs.importRegular(B)
         gemmBitSerial(ctx)
@@ -56,9 +56,13 @@ def test_tc_small_first():
 ENCS = [(1, "u"), (1, "b"), (2, "u"), (2, "s"), (3, "u"), (3, "s"), (4, "u"), (4, "s")]
 
 
+MODES = [_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS]
+
+
+@pytest.mark.parametrize("mode", MODES, ids=["digits", "pairs"])
 @pytest.mark.parametrize("shape", [(128, 256, 128), (200, 1000, 333), (64, 128, 64), (300, 3000, 129),
-                                   (129, 64, 700)])
-def test_tc_encodings_vs_oracle(shape):
+                                   (129, 64, 700), (256, 512, 520)])
+def test_tc_encodings_vs_oracle(shape, mode):
     M, K, N = shape
     rng = np.random.default_rng(M + K + N)
     for (wa, ea) in ENCS:
@@ -68,15 +72,16 @@ def test_tc_encodings_vs_oracle(shape):
             A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
             B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
             sa, sb = ea != "u", eb != "u"
-            assert np.array_equal(tc_gemm(A, B, wa, wb, sa, sb), O.oracle_gemm(A, B, wa, wb, sa, sb)), \
+            assert np.array_equal(tc_gemm(A, B, wa, wb, sa, sb, pipe=mode), O.oracle_gemm(A, B, wa, wb, sa, sb)), \
                 (shape, wa, ea, wb, eb)
     assert _capi.load().gbs_debug_tc_error() == 0
 
 
+@pytest.mark.parametrize("mode", MODES, ids=["digits", "pairs"])
 @pytest.mark.parametrize("name", sorted(CFG))
-def test_tc_full_size_workloads(name):
+def test_tc_full_size_workloads(name, mode):
     M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
-    assert sha(tc_gemm(A, B, wA, wB, sA, sB, expect_tc=min(M, N) >= 64)) == CFG[name]["sha256"]
+    assert sha(tc_gemm(A, B, wA, wB, sA, sB, expect_tc=min(M, N) >= 64, pipe=mode)) == CFG[name]["sha256"]
 
 
 def test_tc_sums_near_the_exactness_bound():
@@ -86,13 +91,13 @@ def test_tc_sums_near_the_exactness_bound():
     A = np.full((M, K), 15, np.int8)
     B = np.ones((N, K), np.int8)
     B[1::2, ::3] = 0
-    got = tc_gemm(A, B, 4, 1, False, False)
     want = O.oracle_gemm(A, B, 4, 1, False, False, threads=16)
-    assert np.array_equal(got, want)
-    # signed: alternating +-8 * 1 partial sums swing across zero
     A2 = np.where((np.arange(K) // 7) % 2 == 0, -8, 7).astype(np.int8)[None, :].repeat(M, 0)
-    got2 = tc_gemm(A2, B, 4, 1, True, False)
-    assert np.array_equal(got2, O.oracle_gemm(A2, B, 4, 1, True, False, threads=16))
+    want2 = O.oracle_gemm(A2, B, 4, 1, True, False, threads=16)
+    for mode in MODES:
+        assert np.array_equal(tc_gemm(A, B, 4, 1, False, False, pipe=mode), want)
+        # signed: alternating -8 / +7 partial sums swing across zero
+        assert np.array_equal(tc_gemm(A2, B, 4, 1, True, False, pipe=mode), want2)
     assert _capi.load().gbs_debug_tc_error() == 0
 
 
