@@ -41,6 +41,7 @@ SIGNATURES = {
     "gbs_export": (i32, [vp, i32, vp, vp]),
     "gbs_get_planes": (i32, [vp, i32, vp, vp]),
     "gbs_set_pipe": (i32, [vp, i32]),
+    "gbs_set_variant": (i32, [vp, i32]),
     "gbs_gemm_noalloc": (i32, [vp, i32, vp, i32, u64, u64, u64, u64, u64, i32, i32, vp, vp]),
     "gbs_noalloc_scratch_bytes": (u64, []),
     "gbs_adjoint": (i32, [vp, vp, vp, vp, vp]),
@@ -56,6 +57,11 @@ SIGNATURES = {
     "gbs_group_free": (i32, [vp]),
     "gbs_debug_group_poison_tile": (i32, [vp, C.c_uint32]),
     "gbs_pipe_peaks": (i32, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gbs_tune": (i32, [vp, i32, C.POINTER(i32), vp]),
+    "gbs_tuner_save": (i32, [C.c_char_p]),
+    "gbs_tuner_load": (i32, [C.c_char_p, i32]),
+    "gbs_tuner_entries": (i32, []),
+    "gbs_tuner_clear": (i32, []),
     "gbs_last_error": (C.c_char_p, []),
     "gbs_version": (C.c_char_p, []),
     "gbs_debug_fail_alloc_after": (None, [i32]),

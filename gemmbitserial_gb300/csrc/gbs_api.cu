@@ -269,6 +269,14 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
   return GBS_OK;
 }
 
+int gbs_set_variant(gbs_ctx *c, int variant) {
+  if (!c) return fail(GBS_EINVAL, "gbs_set_variant: ctx is NULL");
+  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256))
+    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128 or 256");
+  c->variant = variant;
+  return GBS_OK;
+}
+
 int gbs_set_pipe(gbs_ctx *c, int pipe) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_pipe: ctx is NULL");
   if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_TC_PAIRS) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
@@ -307,9 +315,11 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.wa = (int)c->lhs.nbits;
   sh.wb = (int)c->rhs.nbits;
   const int pipe = effective_pipe(c);
+  const int variant = c->variant >= 0 ? c->variant : (c->pipe == GBS_PIPE_AUTO ? tuned_variant(c, pipe) : -1);
+  sh.tile_cls = (pipe == GBS_PIPE_POPC) ? variant : -1;
   cudaError_t ke;
   if (pipe == GBS_PIPE_TC || pipe == GBS_PIPE_TC_PAIRS) {
-    ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC);
+    ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC, variant);
   } else if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
     if (e.use_xor) {
       // ncols - 2*popc(a^b) = 4*popc(a&b) - rsA - rsB - ncols, rs = bipolar row sums (2*popc - ncols)

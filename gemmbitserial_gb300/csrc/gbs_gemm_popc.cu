@@ -273,7 +273,7 @@ int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap) {
 
 cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
-  const bool skinny = (g.M * g.N <= 32768) || g.N < 16 || g.M < 4;
+  const bool skinny = g.tile_cls < 0 && ((g.M * g.N <= 32768) || g.N < 16 || g.M < 4);
   if (skinny) {
     const uint64_t threads = g.M * g.N * 32;
     gemm_popc_skinny<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(g, e);
@@ -285,7 +285,7 @@ cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t
   t.M = g.M; t.N = g.N; t.wpr = g.wpr; t.a_plane = g.a_plane; t.b_plane = g.b_plane;
   t.a_rows = g.a_rows; t.b_rows = g.b_rows;
   t.wa = g.wa; t.wb = g.wb; t.neg_i = e.neg_i; t.neg_j = e.neg_j; t.shift = e.shift; t.c0 = e.c0;
-  const int cls = popc_tile_class(g.M, g.wa, g.wb, 220 * 1024);
+  const int cls = (g.tile_cls >= 0 && g.tile_cls <= 2) ? g.tile_cls : popc_tile_class(g.M, g.wa, g.wb, 220 * 1024);
   if (e.use_xor) return run_tiled_cls<true>(cls, t, s);
   return run_tiled_cls<false>(cls, t, s);
 }

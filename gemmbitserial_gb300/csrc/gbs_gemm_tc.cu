@@ -158,6 +158,47 @@ __device__ __forceinline__ uint32_t decode4(const uint32_t (&pw)[4], int sh, con
   return (lo & ~m) | (hi & m);
 }
 
+// One tile row of one stage: CNT planes (16 bytes each, `pstride` apart) ->
+// 128 e4m3 bytes written as 8 swizzled 16-byte chunks.  Columns at or past
+// `kvalid` are forced to 0 (needed for bipolar operands, whose zero padding
+// bits would otherwise decode to -1).
+template <int CNT>
+__device__ __forceinline__ void decode_row(const uint8_t *src, uint32_t pstride, const uint32_t (&tab)[4],
+                                           uint8_t *dst, int row, int kvalid) {
+  uint32_t w[CNT][4];
+#pragma unroll
+  for (int p = 0; p < CNT; p++) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(src + p * pstride);
+    w[p][0] = v.x; w[p][1] = v.y; w[p][2] = v.z; w[p][3] = v.w;
+  }
+  const uint32_t v0 = tab[0] & 0xFFu, v1 = (tab[0] >> 8) & 0xFFu;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    uint32_t pw[4];
+#pragma unroll
+    for (int p = 0; p < 4; p++) pw[p] = p < CNT ? w[p][c >> 1] : 0u;
+    uint32_t q[4];
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      const int sh = 16 * (c & 1) + 4 * n;
+      if (CNT == 1) {
+        const uint32_t sp = decode4<1>(pw, sh, tab);
+        q[n] = sp * v1 + (sp ^ 0x01010101u) * v0;
+      } else {
+        q[n] = decode4<CNT>(pw, sh, tab);
+      }
+    }
+    if (kvalid < 128) {
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        const int c0 = 16 * c + 4 * n;
+        if (c0 + 4 > kvalid) q[n] &= c0 >= kvalid ? 0u : (0xFFFFFFFFu >> (8 * (4 - (kvalid - c0))));
+      }
+    }
+    *reinterpret_cast<uint4 *>(dst + ((c ^ (row & 7)) << 4)) = make_uint4(q[0], q[1], q[2], q[3]);
+  }
+}
+
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
@@ -252,7 +293,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!ok) mbar_drain(mma_done, 0);  // issued MMAs finish before TMEM is freed
     }
   } else {
-    // ---------------- decoders: one task = one 16-column chunk of one tile row, then epilogue
+    // ---------------- decoders: each thread owns whole tile rows (all 8 chunks of 16 columns)
     const int d = tid - 64;
     const int rowsA = ntA * kBM, rows = rowsA + ntB * BN;
     for (uint32_t k = 0; k < a.nstages; k++) {
@@ -261,54 +302,23 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (k >= (uint32_t)a.no && !mbar_wait(op_empty + 8 * o, ((k / a.no) - 1) & 1, abort_flag)) break;
       const uint8_t *pk = pk_ring + s * pk_stage;
       uint8_t *op = op_ring + o * op_stage;
-      const uint64_t kbase = (uint64_t)k * 128;  // first column of this stage
-      for (int task = d; task < rows * 8; task += 32 * kDecWarps) {
-        const int r = task >> 3, c = task & 7;
+      // columns of this stage past the real K (only the last stage can have any)
+      const int kvalid = (uint64_t)k * 128 + 128 > a.K ? (int)(a.K - (uint64_t)k * 128) : 128;
+      for (int r = d; r < rows; r += 32 * kDecWarps) {
         const bool isA = r < rowsA;
         const int rr = isA ? r : r - rowsA;
-        const int t = isA ? rr / kBM : rr / BN, row = isA ? rr % kBM : rr % BN;
+        const int t = isA ? rr >> 7 : rr / BN, row = isA ? rr & 127 : rr % BN;
         const TcOperand &P = isA ? a.A : a.B;
-        const int cnt = P.count[t];
-        uint32_t pw[4];
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-          pw[p] = 0u;
-          if (p < cnt) {
-            const int plane = P.first[t] + p;
-            const uint8_t *src = isA ? pk + plane * pk_a : pk + a.wa * pk_a + plane * pk_b;
-            pw[p] = *reinterpret_cast<const uint32_t *>(src + row * kPkRowB + (c >> 1) * 4);
-          }
-        }
-        uint32_t tab[4] = {P.tab[t][0], P.tab[t][1], P.tab[t][2], P.tab[t][3]};
-        uint32_t q[4];
-        const int sh0 = 16 * (c & 1);
-        if (cnt == 1) {
-          // one plane: bytes are 0/1, mapped with two table bytes (bipolar: -1/+1)
-          const uint32_t v0 = tab[0] & 0xFFu, v1 = (tab[0] >> 8) & 0xFFu;
-#pragma unroll
-          for (int n = 0; n < 4; n++) {
-            const uint32_t sp = decode4<1>(pw, sh0 + 4 * n, tab);
-            q[n] = sp * v1 + (sp ^ 0x01010101u) * v0;
-          }
-        } else if (cnt == 2) {
-#pragma unroll
-          for (int n = 0; n < 4; n++) q[n] = decode4<2>(pw, sh0 + 4 * n, tab);
-        } else if (cnt == 3) {
-#pragma unroll
-          for (int n = 0; n < 4; n++) q[n] = decode4<3>(pw, sh0 + 4 * n, tab);
-        } else {
-#pragma unroll
-          for (int n = 0; n < 4; n++) q[n] = decode4<4>(pw, sh0 + 4 * n, tab);
-        }
-        if (P.bip) {  // bipolar zero-padding columns past K stay 0 instead of -1
-#pragma unroll
-          for (int n = 0; n < 4; n++) {
-            const uint64_t c0 = kbase + 16 * c + 4 * n;
-            if (c0 + 4 > a.K) q[n] &= c0 >= a.K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (a.K - c0))));
-          }
-        }
+        const uint8_t *src = isA ? pk + P.first[t] * pk_a : pk + a.wa * pk_a + P.first[t] * pk_b;
+        const uint32_t pstride = isA ? pk_a : pk_b;
         uint8_t *dst = op + (isA ? t * a_tile : ntA * a_tile + t * b_tile) + row * kRowB;
-        *reinterpret_cast<uint4 *>(dst + ((c ^ (row & 7)) << 4)) = make_uint4(q[0], q[1], q[2], q[3]);
+        const uint32_t tab[4] = {P.tab[t][0], P.tab[t][1], P.tab[t][2], P.tab[t][3]};
+        switch (P.count[t]) {
+          case 1: decode_row<1>(src + row * kPkRowB, pstride, tab, dst, row, P.bip ? kvalid : 128); break;
+          case 2: decode_row<2>(src + row * kPkRowB, pstride, tab, dst, row, P.bip ? kvalid : 128); break;
+          case 3: decode_row<3>(src + row * kPkRowB, pstride, tab, dst, row, P.bip ? kvalid : 128); break;
+          default: decode_row<4>(src + row * kPkRowB, pstride, tab, dst, row, P.bip ? kvalid : 128); break;
+        }
       }
       // generic-proxy writes become visible to tcgen05.mma (async proxy) via fence + mbarrier release
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -505,7 +515,7 @@ bool tc_supported(const gbs_ctx *c) {
   return encode_fn() != nullptr;
 }
 
-cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits) {
+cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn_req) {
   if (!c->tc_maps_ready) {
     if (!make_plane_map(reinterpret_cast<CUtensorMap *>(c->tc_map_a), c->lhs) ||
         !make_plane_map(reinterpret_cast<CUtensorMap *>(c->tc_map_b), c->rhs))
@@ -526,7 +536,7 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits) {
   a.wb = (int)B.nbits;
   a.A = make_operand(A, digits);
   a.B = make_operand(B, digits);
-  const int bn = (digits && a.N > 128) ? 256 : 128;
+  const int bn = (bn_req == 128 || bn_req == 256) ? bn_req : ((digits && a.N > 128) ? 256 : 128);
   // kind::f8f6f4: D fp32, A and B e4m3, both K-major, M = 128, N = bn
   a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
   int no = 4;

@@ -81,6 +81,7 @@ struct GemmShape {
   uint64_t M, N, wpr;
   uint64_t a_plane, b_plane;  // words per plane (nrows_a * wpr)
   uint64_t a_rows, b_rows;    // padded rows (nrows_a) of lhs and rhs
+  int tile_cls;               // CUDA-core tile class override (0..2), -1 = built-in rule
   int wa, wb;
 };
 
@@ -95,6 +96,7 @@ struct gbs_ctx {
   size_t stage_bytes = 0;
   int device = 0;
   int pipe = GBS_PIPE_AUTO;
+  int variant = -1;  // pipe variant: CUDA-core tile class (0..2) or tensor-core N tile (128/256); -1 = built-in rule
   // TMA descriptors (CUtensorMap, 128 bytes, 64-byte aligned) over the planes, built on first use
   alignas(64) unsigned char tc_map_a[128];
   alignas(64) unsigned char tc_map_b[128];
@@ -131,9 +133,10 @@ cudaError_t launch_rowsum_grouped(const PackJob *jobs, int njobs, uint64_t total
 cudaError_t launch_gemm_bmma(const GemmShape &g, const Epilogue &e, cudaStream_t s);
 bool bmma_supported(int wa, int wb, int use_xor);
 bool tc_supported(const gbs_ctx *c);
-cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits);
+cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 int effective_pipe(const gbs_ctx *c);
+int tuned_variant(const gbs_ctx *c, int pipe);
 
 }  // namespace gbs

@@ -133,6 +133,7 @@ extern "C" int gbs_gemm_noalloc(const void *lhs, int lhs_dtype, const void *rhs,
   sh.b_rows = c.rhs.nrows_a;
   sh.wa = (int)lhsBits;
   sh.wb = (int)rhsBits;
+  sh.tile_cls = -1;
   e = launch_gemm_popc(sh, ep, s);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_gemm_noalloc: forward kernel");
   return GBS_OK;

@@ -9,6 +9,12 @@
 //     accumulators.
 // Both loops run on every SM (4 CTAs of 256 threads each) for ~10-20 ms.
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 
 #include "gbs_internal.h"
 
@@ -82,14 +88,105 @@ __global__ void __launch_bounds__(256) peak_fma(const float *in, float *out, int
 
 }  // namespace
 
+namespace {
+
+// ---------------------------------------------------------------- tuner store
+// Key: shape class (log4 buckets of M, N and K, capped), widths and encodings
+// (0 unsigned, 1 signed, 2 bipolar).  Value: the fastest pipe and variant
+// measured by gbs_tune on this device.
+constexpr const char *kStoreVersion = "gbs-tuner v1 sm_103a";
+
+typedef std::tuple<int, int, int, int, int, int, int> TuneKey;
+struct TuneChoice {
+  int pipe, variant;
+  double us;
+};
+std::map<TuneKey, TuneChoice> g_store;
+std::mutex g_store_mu;
+bool g_env_loaded = false;
+
+int bucket(uint64_t x) {
+  int b = 0;
+  while (x >= 4 && b < 8) {
+    x >>= 2;
+    b++;
+  }
+  return b;
+}
+int enc_of(const Mat &m) { return m.bipolar() ? 2 : (m.issigned ? 1 : 0); }
+
+TuneKey key_of(const gbs_ctx *c) {
+  return TuneKey(bucket(c->lhs.nrows), bucket(c->rhs.nrows), bucket(c->lhs.ncols), (int)c->lhs.nbits,
+                 (int)c->rhs.nbits, enc_of(c->lhs), enc_of(c->rhs));
+}
+
+int load_store(const char *path, bool replace);
+
+void load_env_store() {
+  if (g_env_loaded) return;
+  g_env_loaded = true;
+  const char *p = getenv("GBS_TUNER_STORE");
+  if (p && *p) load_store(p, false);
+}
+
+}  // namespace
+
 // Measured on GB300: the CUDA-core POPC pipe sustains ~160 T bit-op/s and the
 // b1 mma.sync pipe about half that (gbs_pipe_peaks), while tcgen05 e4m3
-// multiply-adds run at ~1.75 P/s (gbs_tc_peaks).  So every shape the
-// tensor-core pipe covers exactly goes there; the rest (8-bit widths, more
-// than 5 planes, K beyond the fp32-exact bound, skinny shapes) use the CUDA
-// cores.  The b1 pipe is never the better choice on this GPU.
-int choose_pipe(const gbs_ctx *c) { return tc_supported(c) ? GBS_PIPE_TC : GBS_PIPE_POPC; }
+// multiply-adds run at ~1.75 P/s (gbs_tc_peaks).  Without a tuner entry,
+// every shape the tensor-core pipe covers exactly goes there; the rest
+// (8-bit widths, more than 5 planes, K beyond the fp32-exact bound, skinny
+// shapes) use the CUDA cores.  A tuner entry for the shape class wins when
+// its pipe applies to this context.
+int choose_pipe(const gbs_ctx *c) {
+  {
+    std::lock_guard<std::mutex> lock(g_store_mu);
+    load_env_store();
+    auto it = g_store.find(key_of(c));
+    if (it != g_store.end()) {
+      const int p = it->second.pipe;
+      if (p == GBS_PIPE_POPC || p == GBS_PIPE_BMMA) return p;
+      if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS) && tc_supported(c)) return p;
+    }
+  }
+  return tc_supported(c) ? GBS_PIPE_TC : GBS_PIPE_POPC;
+}
 
+int tuned_variant(const gbs_ctx *c, int pipe) {
+  std::lock_guard<std::mutex> lock(g_store_mu);
+  auto it = g_store.find(key_of(c));
+  return (it != g_store.end() && it->second.pipe == pipe) ? it->second.variant : -1;
+}
+
+namespace {
+
+int load_store(const char *path, bool replace) {
+  FILE *f = fopen(path, "r");
+  if (!f) return fail(GBS_EINVAL, std::string("gbs_tuner_load: cannot open ") + path);
+  char line[256];
+  if (!fgets(line, sizeof(line), f) || strncmp(line, kStoreVersion, strlen(kStoreVersion)) != 0) {
+    fclose(f);
+    return fail(GBS_EINVAL, "gbs_tuner_load: store written by another version; entries ignored");
+  }
+  std::map<TuneKey, TuneChoice> fresh;
+  int n = 0;
+  while (fgets(line, sizeof(line), f)) {
+    int k[7], pipe, variant;
+    double us;
+    if (sscanf(line, "%d %d %d %d %d %d %d %d %d %lf", &k[0], &k[1], &k[2], &k[3], &k[4], &k[5], &k[6], &pipe,
+               &variant, &us) != 10)
+      continue;
+    if (pipe < GBS_PIPE_POPC || pipe > GBS_PIPE_TC_PAIRS) continue;
+    fresh[TuneKey(k[0], k[1], k[2], k[3], k[4], k[5], k[6])] = TuneChoice{pipe, variant, us};
+    n++;
+  }
+  fclose(f);
+  if (replace) g_store.clear();
+  for (auto &kv : fresh) g_store[kv.first] = kv.second;
+  return GBS_OK;
+}
+
+}  // namespace
 }  // namespace gbs
 
 using namespace gbs;
@@ -180,5 +277,90 @@ extern "C" int gbs_fma_peak(double *flops) {
   cudaFree(out);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_fma_peak");
   if (flops) *flops = 2.0 * blocks * threads * (double)iters * 8.0 / (best * 1e-3);
+  return GBS_OK;
+}
+
+extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_tune: ctx is NULL");
+  if (!c->lhs.imported || !c->rhs.imported) return fail(GBS_ESTATE, "gbs_tune: import both operands first");
+  if (reps < 1) reps = 3;
+  cudaStream_t s = (cudaStream_t)stream;
+  struct Cand {
+    int pipe, variant;
+  };
+  Cand cands[12];
+  int nc = 0;
+  for (int v = -1; v <= 2; v++) cands[nc++] = Cand{GBS_PIPE_POPC, v};  // -1: built-in tile rule
+  cands[nc++] = Cand{GBS_PIPE_BMMA, -1};
+  if (tc_supported(c)) {
+    cands[nc++] = Cand{GBS_PIPE_TC, 128};
+    cands[nc++] = Cand{GBS_PIPE_TC, 256};
+    cands[nc++] = Cand{GBS_PIPE_TC_PAIRS, 128};
+  }
+  const int saved_pipe = c->pipe, saved_variant = c->variant;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  TuneChoice best{GBS_PIPE_POPC, -1, 1e30};
+  int rc = GBS_OK;
+  for (int i = 0; i < nc && rc == GBS_OK; i++) {
+    c->pipe = cands[i].pipe;
+    c->variant = cands[i].variant;
+    rc = gbs_gemm(c, stream);  // warm-up (also builds tensor maps)
+    if (rc != GBS_OK) break;
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps && rc == GBS_OK; r++) rc = gbs_gemm(c, stream);
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "gbs_tune: timing");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double us = 1e3 * ms / reps;
+    if (us < best.us) best = TuneChoice{cands[i].pipe, cands[i].variant, us};
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->pipe = saved_pipe;
+  c->variant = saved_variant;
+  if (rc != GBS_OK) return rc;
+  {
+    std::lock_guard<std::mutex> lock(g_store_mu);
+    g_store[key_of(c)] = best;
+  }
+  if (best_pipe) *best_pipe = best.pipe;
+  return GBS_OK;
+}
+
+extern "C" int gbs_tuner_save(const char *path) {
+  if (!path) return fail(GBS_EINVAL, "gbs_tuner_save: path is NULL");
+  std::lock_guard<std::mutex> lock(g_store_mu);
+  FILE *f = fopen(path, "w");
+  if (!f) return fail(GBS_EINVAL, std::string("gbs_tuner_save: cannot open ") + path);
+  fprintf(f, "%s\n", kStoreVersion);
+  for (auto &kv : g_store) {
+    const TuneKey &k = kv.first;
+    fprintf(f, "%d %d %d %d %d %d %d %d %d %.3f\n", std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k),
+            std::get<4>(k), std::get<5>(k), std::get<6>(k), kv.second.pipe, kv.second.variant, kv.second.us);
+  }
+  fclose(f);
+  return GBS_OK;
+}
+
+extern "C" int gbs_tuner_load(const char *path, int replace) {
+  if (!path) return fail(GBS_EINVAL, "gbs_tuner_load: path is NULL");
+  std::lock_guard<std::mutex> lock(g_store_mu);
+  return load_store(path, replace != 0);
+}
+
+extern "C" int gbs_tuner_entries(void) {
+  std::lock_guard<std::mutex> lock(g_store_mu);
+  return (int)g_store.size();
+}
+
+extern "C" int gbs_tuner_clear(void) {
+  std::lock_guard<std::mutex> lock(g_store_mu);
+  g_store.clear();
   return GBS_OK;
 }

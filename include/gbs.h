@@ -137,6 +137,11 @@ GBS_API int gbs_export(gbs_ctx *ctx, int side, int32_t *dst, void *stream);
  * after the copy has completed. */
 GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
 
+/* Forces the variant of a context's pipe: CUDA-core tile class (0: 64x64,
+ * 1: 32x128, 2: 16x256 outputs per CTA) or tensor-core N tile (128 or 256);
+ * -1 restores the built-in rule.  No reference counterpart. */
+GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
+
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
 GBS_API int gbs_set_pipe(gbs_ctx *ctx, int pipe);
 
@@ -230,6 +235,22 @@ GBS_API int gbs_tc_peaks(double *f8_flops, double *bf16_flops);
 /* Measures the sustained FP32 FMA rate (FLOP/s, 2 per FMA) of the current
  * device, the roofline of gbs_adjoint (~20 ms).  No reference counterpart. */
 GBS_API int gbs_fma_peak(double *flops);
+
+/* ---- autotuner ----------------------------------------------------------- *
+ * No reference counterpart (the reference picks cache blocks analytically,
+ * gemmbitserial.hpp:343-377).  gbs_tune times every pipe and variant that
+ * applies to an imported context on `stream` (reps timed calls each) and
+ * records the fastest for the context's shape class (log4 buckets of M, N,
+ * K), widths and encodings; GBS_PIPE_AUTO contexts of that class then use
+ * it.  The store persists through gbs_tuner_save / gbs_tuner_load (a
+ * versioned text file; a file from another version is rejected and its
+ * entries ignored).  The library also loads the file named by the
+ * environment variable GBS_TUNER_STORE on first use. */
+GBS_API int gbs_tune(gbs_ctx *ctx, int reps, int *best_pipe, void *stream);
+GBS_API int gbs_tuner_save(const char *path);
+GBS_API int gbs_tuner_load(const char *path, int replace);
+GBS_API int gbs_tuner_entries(void);
+GBS_API int gbs_tuner_clear(void);
 
 /* Message describing the last failure on the calling thread ("" if none). */
 GBS_API const char *gbs_last_error(void);

@@ -1,0 +1,86 @@
+"""gbs_tune: times every applicable pipe/variant on a context's own data,
+records the winner for its shape class, and the automatic choice follows it;
+results stay bit-exact whatever the choice."""
+import ctypes as C
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gemmbitserial_gb300 import _capi, datagen
+from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext, gemmBitSerial
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_tune_records_winner_and_stays_exact(gbs_lib, tmp_path):
+    lib = gbs_lib
+    lib.gbs_tuner_clear()
+    cfg = json.load(open(os.path.join(GOLD, "ref_configs.json")))
+    for name in ["gemm_2048x4096x2048_u3s2", "gemm_256x9216x4096_bpbp"]:
+        M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+        ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        best = C.c_int()
+        _capi.check(lib.gbs_tune(ctx._h, 3, C.byref(best), None))
+        assert best.value in (_capi.GBS_PIPE_POPC, _capi.GBS_PIPE_BMMA, _capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS)
+        assert ctx.pipe == best.value  # AUTO follows the store
+        gemmBitSerial(ctx)
+        got = ctx.res.reshape(N, M)
+        assert hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest() == cfg[name]["sha256"]
+        deallocGEMMContext(ctx)
+    assert lib.gbs_tuner_entries() == 2
+    path = str(tmp_path / "store.txt").encode()
+    _capi.check(lib.gbs_tuner_save(path))
+    lib.gbs_tuner_clear()
+    _capi.check(lib.gbs_tuner_load(path, 1))
+    assert lib.gbs_tuner_entries() == 2
+    lib.gbs_tuner_clear()
+
+
+CANDIDATES = [(_capi.GBS_PIPE_POPC, v) for v in (-1, 0, 1, 2)] + [(_capi.GBS_PIPE_BMMA, -1)] + \
+    [(_capi.GBS_PIPE_TC, 128), (_capi.GBS_PIPE_TC, 256), (_capi.GBS_PIPE_TC_PAIRS, 128), (_capi.GBS_PIPE_TC_PAIRS, 256)]
+
+
+def test_every_candidate_is_exact(gbs_lib):
+    """Every (pipe, variant) the tuner may pick gives the oracle's result."""
+    lib = gbs_lib
+    rng = np.random.default_rng(8)
+    for (M, K, N, wa, ea, wb, eb) in [(300, 1000, 500, 3, "u", 2, "s"), (130, 640, 260, 1, "b", 1, "b")]:
+        A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+        B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+        want = O.oracle_gemm(A, B, wa, wb, ea != "u", eb != "u")
+        ctx = allocGEMMContext(M, K, N, wa, wb, ea != "u", eb != "u")
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        for pipe, var in CANDIDATES:
+            _capi.check(lib.gbs_set_pipe(ctx._h, pipe))
+            _capi.check(lib.gbs_set_variant(ctx._h, var))
+            gemmBitSerial(ctx)
+            assert np.array_equal(ctx.res.reshape(N, M), want), (M, K, N, pipe, var)
+        deallocGEMMContext(ctx)
+
+
+def test_tuned_variants_are_exact(gbs_lib):
+    """The tuner's pick gives the oracle's result."""
+    lib = gbs_lib
+    rng = np.random.default_rng(9)
+    for (M, K, N, wa, ea, wb, eb) in [(300, 1000, 500, 3, "u", 2, "s"), (40, 2000, 700, 1, "b", 4, "s"),
+                                      (130, 640, 260, 2, "s", 2, "u")]:
+        A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+        B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+        want = O.oracle_gemm(A, B, wa, wb, ea != "u", eb != "u")
+        ctx = allocGEMMContext(M, K, N, wa, wb, ea != "u", eb != "u")
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        best = C.c_int()
+        _capi.check(lib.gbs_tune(ctx._h, 1, C.byref(best), None))
+        gemmBitSerial(ctx)
+        assert np.array_equal(ctx.res.reshape(N, M), want), (M, K, N, best.value)
+        deallocGEMMContext(ctx)
+    lib.gbs_tuner_clear()
