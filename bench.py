@@ -438,11 +438,11 @@ def run_ours(args):
         return
     # ---- roofline of the forward kernel against the measured peak of the pipe it ran on
     kpad = (K + 63) // 64 * 64
-    if pipe in (_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS):
+    if pipe in (_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS, _capi.GBS_PIPE_TC_SMEM):
         f8, bf16 = C.c_double(), C.c_double()
         _capi.check(lib.gbs_tc_peaks(C.byref(f8), C.byref(bf16)))
-        kernel = "gemm_tc_kernel"
-        digits = pipe == _capi.GBS_PIPE_TC
+        kernel = "gemm_tc_tma_kernel" if pipe == _capi.GBS_PIPE_TC else "gemm_tc_kernel"
+        digits = pipe != _capi.GBS_PIPE_TC_PAIRS
         # fp8 multiply-adds the tensor pipe must do: one per (m, n, k) in digit mode, one per plane pair otherwise
         work = 2.0 * M * N * K * (1 if digits else wA * wB)
         achieved = work / (ms * 1e-3) / 1e12
@@ -482,7 +482,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded splitmix64)",
             "config": dict(desc, parallelism=f"replicas x{world}", l2="flushed before every step (256 MiB write, outside the timed events)",
-                           pipe={1: "popc", 2: "bmma", 3: "tcgen05-digits", 4: "tcgen05-pairs"}.get(pipe, str(pipe))),
+                           pipe={1: "popc", 2: "bmma", 3: "tcgen05 (HBM digits, TMA)", 4: "tcgen05 (smem plane pairs)",
+                                 5: "tcgen05 (smem digits)"}.get(pipe, str(pipe))),
             "parity": parity,
             "e2e": {"value": round(gops(M, K, N, e2e_s) * world, 3), "unit": "GOPS",
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),

@@ -13,7 +13,7 @@ from . import build as _build
 GBS_OK, GBS_EINVAL, GBS_ENOMEM, GBS_ECUDA, GBS_ESTATE, GBS_ETIMEOUT, GBS_EUNSUPPORTED = range(7)
 GBS_I8, GBS_U8, GBS_I16, GBS_I32 = range(4)
 GBS_LHS, GBS_RHS = 0, 1
-GBS_PIPE_AUTO, GBS_PIPE_POPC, GBS_PIPE_BMMA, GBS_PIPE_TC, GBS_PIPE_TC_PAIRS = 0, 1, 2, 3, 4
+GBS_PIPE_AUTO, GBS_PIPE_POPC, GBS_PIPE_BMMA, GBS_PIPE_TC, GBS_PIPE_TC_PAIRS, GBS_PIPE_TC_SMEM = 0, 1, 2, 3, 4, 5
 
 # Every entry point include/gbs.h declares, with (restype, argtypes).
 u64, i32, vp = C.c_uint64, C.c_int, C.c_void_p

@@ -80,6 +80,8 @@ void free_ctx_buffers(gbs_ctx *c) {
   if (c->res) cudaFree(c->res);
   if (c->rowsum) cudaFree(c->rowsum);
   if (c->stage) cudaFree(c->stage);
+  if (c->digits[0]) cudaFree(c->digits[0]);
+  if (c->digits[1]) cudaFree(c->digits[1]);
 }
 
 // Epilogue and operand order for one context (see gbs_internal.h: Epilogue).
@@ -120,7 +122,7 @@ int choose_pipe(const gbs_ctx *c);
 // the CUDA cores for shapes it does not cover.
 int effective_pipe(const gbs_ctx *c) {
   const int p = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
-  if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS) && !tc_supported(c)) return GBS_PIPE_POPC;
+  if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && !tc_supported(c)) return GBS_PIPE_POPC;
   return p;
 }
 
@@ -266,6 +268,7 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
     if (pe != cudaSuccess) return cuda_fail(pe, "gbs_import: pack kernel");
   }
   m.imported = true;
+  c->digits_valid[side] = false;  // the digit matrix of this side is rebuilt from the new planes
   return GBS_OK;
 }
 
@@ -279,7 +282,7 @@ int gbs_set_variant(gbs_ctx *c, int variant) {
 
 int gbs_set_pipe(gbs_ctx *c, int pipe) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_pipe: ctx is NULL");
-  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_TC_PAIRS) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
+  if (pipe < GBS_PIPE_AUTO || pipe > GBS_PIPE_TC_SMEM) return fail(GBS_EINVAL, "gbs_set_pipe: unknown pipe");
   c->pipe = pipe;
   return GBS_OK;
 }
@@ -318,8 +321,10 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   const int variant = c->variant >= 0 ? c->variant : (c->pipe == GBS_PIPE_AUTO ? tuned_variant(c, pipe) : -1);
   sh.tile_cls = (pipe == GBS_PIPE_POPC) ? variant : -1;
   cudaError_t ke;
-  if (pipe == GBS_PIPE_TC || pipe == GBS_PIPE_TC_PAIRS) {
-    ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC, variant);
+  if (pipe == GBS_PIPE_TC) {
+    ke = launch_gemm_tc_hbm(c, s, variant);
+  } else if (pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM) {
+    ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC_SMEM, variant);
   } else if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
     if (e.use_xor) {
       // ncols - 2*popc(a^b) = 4*popc(a&b) - rsA - rsB - ncols, rs = bipolar row sums (2*popc - ncols)

@@ -364,6 +364,170 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// ---------------------------------------------------------------- HBM digit path
+// Expansion: one thread per 16 columns of one padded row writes the row's
+// e4m3 digits (16 bytes) of operand planes -> digit matrix [nrows_a][ncols_a].
+// Rows past nrows and columns past K are 0, so padding never contributes.
+template <int CNT>
+__global__ void __launch_bounds__(256) expand_digits_kernel(const uint64_t *__restrict__ planes,
+                                                            uint8_t *__restrict__ out, uint64_t nrows,
+                                                            uint64_t nrows_a, uint64_t K, uint64_t ncols_a,
+                                                            uint64_t wpr, uint4 tabv) {
+  const uint64_t chunks = ncols_a / 16;
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows_a * chunks) return;
+  const uint64_t r = i / chunks, col0 = (i % chunks) * 16;
+  uint4 res = make_uint4(0u, 0u, 0u, 0u);
+  if (r < nrows && col0 < K) {
+    const uint64_t w = col0 >> 6;
+    const int sh = (int)(col0 & 63);
+    uint32_t pw[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int p = 0; p < CNT; p++) pw[p] = (uint32_t)(planes[p * nrows_a * wpr + r * wpr + w] >> (sh & 32));
+    const uint32_t tab[4] = {tabv.x, tabv.y, tabv.z, tabv.w};
+    uint32_t q[4];
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      const int s4 = (sh & 16) + 4 * n;
+      if (CNT == 1) {
+        const uint32_t sp = decode4<1>(pw, s4, tab);
+        q[n] = sp * ((tab[0] >> 8) & 0xFFu) + (sp ^ 0x01010101u) * (tab[0] & 0xFFu);
+      } else {
+        q[n] = decode4<CNT>(pw, s4, tab);
+      }
+      const uint64_t c0 = col0 + 4 * n;
+      if (c0 + 4 > K) q[n] &= c0 >= K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (K - c0))));
+    }
+    res = make_uint4(q[0], q[1], q[2], q[3]);
+  }
+  *reinterpret_cast<uint4 *>(out + r * ncols_a + col0) = res;
+}
+
+// TMA-fed GEMM on digit matrices: 128 x BN output tile per CTA.
+//   warp 0     TMA: A box 128 rows x 128 bytes, B boxes 128 rows x 128 bytes
+//              (BN/128 of them), 128-byte swizzle = the MMA's K-major layout
+//   warp 1     TMEM allocation; lane 0 issues 4 tcgen05.mma (K = 32) per stage
+//   warps 2-9  epilogue: TMEM -> int32 -> res[n*M + m]
+constexpr int kTmaStagesMax = 4;
+constexpr int kTmaThreads = 320;
+
+struct TmaArgs {
+  int32_t *C;
+  uint64_t M, N;
+  uint32_t nstages;
+  uint32_t idesc;
+  int stages;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kTmaThreads, 1)
+    gemm_tc_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TmaArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t a_bytes = kBM * kRowB, b_bytes = BN * kRowB, stage_bytes = a_bytes + b_bytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.stages * stage_bytes);
+  const uint32_t full = smem_u32(bars), empty = full + 8 * a.stages, acc_full = empty + 8 * a.stages;
+  const uint32_t mma_done = acc_full + 8;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * a.stages + 2);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const uint64_t m0 = (uint64_t)blockIdx.x * kBM, n0 = (uint64_t)blockIdx.y * BN;
+
+  if (tid == 0) {
+    for (int i = 0; i < a.stages; i++) {
+      mbar_init(full + 8 * i, 1);
+      mbar_init(empty + 8 * i, 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "n"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t issued = 0;
+      for (uint32_t k = 0; k < a.nstages; k++) {
+        const uint32_t s = k % a.stages, use = k / a.stages;
+        if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) break;
+        mbar_expect_tx(full + 8 * s, stage_bytes);
+        const uint32_t dst = smem_u32(smem + s * stage_bytes);
+        tma_load_2d(dst, &tmA, (int)(k * 128), (int)m0, full + 8 * s);
+        for (int h = 0; h < BN / 128; h++)
+          tma_load_2d(dst + a_bytes + h * 128 * kRowB, &tmB, (int)(k * 128), (int)(n0 + 128 * h), full + 8 * s);
+        issued = k + 1;
+      }
+      if (*abort_flag) {
+        for (uint32_t k = (issued > (uint32_t)a.stages ? issued - a.stages : 0); k < issued; k++)
+          mbar_drain(full + 8 * (k % a.stages), (k / a.stages) & 1);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      bool ok = true;
+      for (uint32_t k = 0; k < a.nstages && ok; k++) {
+        const uint32_t s = k % a.stages;
+        if (!mbar_wait(full + 8 * s, (k / a.stages) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t base = smem_u32(smem + s * stage_bytes);
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+          mma_f8(tmem, sw128_desc(base + kk * 32), sw128_desc(base + a_bytes + kk * 32), a.idesc, (k | kk) != 0);
+        mma_commit(empty + 8 * s);
+      }
+      mma_commit(ok ? acc_full : mma_done);
+      if (!ok) mbar_drain(mma_done, 0);
+    }
+  } else {
+    if (__all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag))) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int quarter = warp & 3, half = (warp - 2) >> 2;
+      const uint64_t gm = m0 + quarter * 32 + lane;
+#pragma unroll 1
+      for (int cb = 0; cb < BN / 64; cb++) {
+        const int col = half * (BN / 2) + cb * 32;
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)col;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+              "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+              "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (gm < a.M) {
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const uint64_t gn = n0 + col + j;
+            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(BN));
+  }
+}
+
 // Throughput probe: one CTA per SM, one thread issuing back-to-back
 // tcgen05.mma (M=128, N=256) from fixed zeroed shared tiles; kind 0 = e4m3
 // (K=32), kind 1 = bf16 (K=16).  A commit + bounded wait closes every 64 MMAs.
@@ -557,6 +721,89 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn_req) 
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + 127) / 128));
     gemm_tc_kernel<128><<<grid, kThreads, smem, s>>>(ma, mb, a);
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+namespace {
+
+// Tensor map over a digit matrix: 2-D u8 [nrows_a][ncols_a], box 128 x 128, 128-byte swizzle.
+bool make_digit_map(CUtensorMap *map, const uint8_t *digits, const Mat &m) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {m.ncols_a, m.nrows_a};
+  cuuint64_t strides[1] = {m.ncols_a};
+  cuuint32_t box[2] = {128, 128};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void *)digits, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
+  Mat &m = side ? c->rhs : c->lhs;
+  if (!c->digits[side]) {
+    cudaError_t e = dev_alloc((void **)&c->digits[side], m.nrows_a * m.ncols_a);
+    if (e != cudaSuccess) return e;
+    c->digit_maps_ready = false;
+  }
+  const TcOperand op = make_operand(m, true);
+  const uint4 tab = make_uint4(op.tab[0][0], op.tab[0][1], op.tab[0][2], op.tab[0][3]);
+  const uint64_t threads = m.nrows_a * (m.ncols_a / 16);
+  const unsigned blocks = (unsigned)((threads + 255) / 256);
+  switch (m.nbits) {
+    case 1: expand_digits_kernel<1><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
+    case 2: expand_digits_kernel<2><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
+    case 3: expand_digits_kernel<3><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
+    default: expand_digits_kernel<4><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
+  }
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) c->digits_valid[side] = true;
+  return e;
+}
+
+}  // namespace
+
+cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
+  for (int side = 0; side < 2; side++)
+    if (!c->digits_valid[side]) {
+      cudaError_t e = expand_side(c, side, s);
+      if (e != cudaSuccess) return e;
+    }
+  if (!c->digit_maps_ready) {
+    if (!make_digit_map(reinterpret_cast<CUtensorMap *>(c->tc_map_da), c->digits[0], c->lhs) ||
+        !make_digit_map(reinterpret_cast<CUtensorMap *>(c->tc_map_db), c->digits[1], c->rhs))
+      return cudaErrorInvalidValue;
+    c->digit_maps_ready = true;
+  }
+  TmaArgs a;
+  memset(&a, 0, sizeof(a));
+  a.C = c->res;
+  a.M = c->lhs.nrows;
+  a.N = c->rhs.nrows;
+  a.nstages = (uint32_t)(c->lhs.ncols_a / 128);
+  const int bn = (bn_req == 128 || bn_req == 256) ? bn_req : (a.N > 128 ? 256 : 128);
+  a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+  const size_t stage_bytes = (size_t)(kBM + bn) * kRowB;
+  int stages = kTmaStagesMax;
+  while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 > kSmemCap) stages--;
+  a.stages = stages;
+  const size_t smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16;
+  const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
+  const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_db);
+  cudaError_t e;
+  if (bn == 256) {
+    e = cudaFuncSetAttribute(gemm_tc_tma_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + 255) / 256));
+    gemm_tc_tma_kernel<256><<<grid, kTmaThreads, smem, s>>>(ma, mb, a);
+  } else {
+    e = cudaFuncSetAttribute(gemm_tc_tma_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((a.M + kBM - 1) / kBM), (unsigned)((a.N + 127) / 128));
+    gemm_tc_tma_kernel<128><<<grid, kTmaThreads, smem, s>>>(ma, mb, a);
   }
   count_launch();
   return cudaGetLastError();

@@ -101,6 +101,13 @@ struct gbs_ctx {
   alignas(64) unsigned char tc_map_a[128];
   alignas(64) unsigned char tc_map_b[128];
   bool tc_maps_ready = false;
+  // e4m3 digit matrices [nrows_a][ncols_a] of both operands (the tensor-core
+  // pipe's operands), built from the planes on first use after each import
+  uint8_t *digits[2] = {nullptr, nullptr};
+  bool digits_valid[2] = {false, false};
+  alignas(64) unsigned char tc_map_da[128];
+  alignas(64) unsigned char tc_map_db[128];
+  bool digit_maps_ready = false;
 };
 
 namespace gbs {
@@ -134,6 +141,7 @@ cudaError_t launch_gemm_bmma(const GemmShape &g, const Epilogue &e, cudaStream_t
 bool bmma_supported(int wa, int wb, int use_xor);
 bool tc_supported(const gbs_ctx *c);
 cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
+cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 int effective_pipe(const gbs_ctx *c);

@@ -146,7 +146,7 @@ int choose_pipe(const gbs_ctx *c) {
     if (it != g_store.end()) {
       const int p = it->second.pipe;
       if (p == GBS_PIPE_POPC || p == GBS_PIPE_BMMA) return p;
-      if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS) && tc_supported(c)) return p;
+      if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && tc_supported(c)) return p;
     }
   }
   return tc_supported(c) ? GBS_PIPE_TC : GBS_PIPE_POPC;
@@ -176,7 +176,7 @@ int load_store(const char *path, bool replace) {
     if (sscanf(line, "%d %d %d %d %d %d %d %d %d %lf", &k[0], &k[1], &k[2], &k[3], &k[4], &k[5], &k[6], &pipe,
                &variant, &us) != 10)
       continue;
-    if (pipe < GBS_PIPE_POPC || pipe > GBS_PIPE_TC_PAIRS) continue;
+    if (pipe < GBS_PIPE_POPC || pipe > GBS_PIPE_TC_SMEM) continue;
     fresh[TuneKey(k[0], k[1], k[2], k[3], k[4], k[5], k[6])] = TuneChoice{pipe, variant, us};
     n++;
   }
@@ -288,13 +288,14 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
   struct Cand {
     int pipe, variant;
   };
-  Cand cands[12];
+  Cand cands[16];
   int nc = 0;
   for (int v = -1; v <= 2; v++) cands[nc++] = Cand{GBS_PIPE_POPC, v};  // -1: built-in tile rule
   cands[nc++] = Cand{GBS_PIPE_BMMA, -1};
   if (tc_supported(c)) {
     cands[nc++] = Cand{GBS_PIPE_TC, 128};
     cands[nc++] = Cand{GBS_PIPE_TC, 256};
+    cands[nc++] = Cand{GBS_PIPE_TC_SMEM, 256};
     cands[nc++] = Cand{GBS_PIPE_TC_PAIRS, 128};
   }
   const int saved_pipe = c->pipe, saved_variant = c->variant;

@@ -59,9 +59,11 @@ enum {
   GBS_PIPE_AUTO = 0, /* per-shape choice (tuner store, else built-in rule) */
   GBS_PIPE_POPC = 1, /* CUDA cores: LOP3 AND/XOR + POPC */
   GBS_PIPE_BMMA = 2, /* tensor pipe: mma.sync b1 AND/XOR + popc */
-  GBS_PIPE_TC = 3,   /* 5th-gen tensor cores, digit mode: each operand's planes decode to one fp8
-                        value tile, so one tcgen05.mma sums every plane pair */
-  GBS_PIPE_TC_PAIRS = 4 /* 5th-gen tensor cores, one tcgen05.mma per plane pair, fp8 {0, +-2^i} */
+  GBS_PIPE_TC = 3,       /* 5th-gen tensor cores: each operand's planes expand once (per import) into an
+                            e4m3 digit matrix in HBM; TMA feeds tcgen05.mma, one MMA sums every plane pair */
+  GBS_PIPE_TC_PAIRS = 4, /* 5th-gen tensor cores: packed planes staged through shared memory by TMA and
+                            decoded per tile to e4m3 {0, +-2^i}; one tcgen05.mma per plane pair */
+  GBS_PIPE_TC_SMEM = 5   /* as GBS_PIPE_TC_PAIRS, but each tile's planes decode to one digit tile */
 };
 
 typedef struct gbs_ctx gbs_ctx; /* opaque; copies of the handle alias one context */

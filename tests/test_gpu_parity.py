@@ -52,7 +52,8 @@ def gpu_gemm(A, B, wA, wB, sA, sB, cmA=False, cmB=False, pipe=None):
         deallocGEMMContext(ctx)
 
 
-PIPES = [_capi.GBS_PIPE_AUTO, _capi.GBS_PIPE_POPC, _capi.GBS_PIPE_BMMA, _capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS]
+PIPES = [_capi.GBS_PIPE_AUTO, _capi.GBS_PIPE_POPC, _capi.GBS_PIPE_BMMA, _capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS,
+         _capi.GBS_PIPE_TC_SMEM]
 
 
 @pytest.mark.parametrize("c", VEC["gemm"], ids=[c["name"] for c in VEC["gemm"]])

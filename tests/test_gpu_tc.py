@@ -56,10 +56,11 @@ def test_tc_small_first():
 ENCS = [(1, "u"), (1, "b"), (2, "u"), (2, "s"), (3, "u"), (3, "s"), (4, "u"), (4, "s")]
 
 
-MODES = [_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS]
+MODES = [_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS]
+MODE_IDS = ["hbm-digits", "smem-digits", "pairs"]
 
 
-@pytest.mark.parametrize("mode", MODES, ids=["digits", "pairs"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 @pytest.mark.parametrize("shape", [(128, 256, 128), (200, 1000, 333), (64, 128, 64), (300, 3000, 129),
                                    (129, 64, 700), (256, 512, 520)])
 def test_tc_encodings_vs_oracle(shape, mode):
@@ -77,7 +78,7 @@ def test_tc_encodings_vs_oracle(shape, mode):
     assert _capi.load().gbs_debug_tc_error() == 0
 
 
-@pytest.mark.parametrize("mode", MODES, ids=["digits", "pairs"])
+@pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
 @pytest.mark.parametrize("name", sorted(CFG))
 def test_tc_full_size_workloads(name, mode):
     M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
@@ -117,3 +118,23 @@ def test_tc_peaks_probe():
     print(f"tcgen05 e4m3 {f8.value / 1e12:.0f} TFLOP/s, bf16 {bf.value / 1e12:.0f} TFLOP/s")
     assert f8.value > 1e14 and bf.value > 1e14
     assert _capi.load().gbs_debug_tc_error() == 0
+
+
+def test_tc_digit_cache_follows_reimport():
+    """The digit matrices are rebuilt after an import changes the planes."""
+    M, K, N = 256, 640, 384
+    A1 = datagen.operand(datagen.SEED_BASE + 610, M, K, 2, "u")
+    A2 = datagen.operand(datagen.SEED_BASE + 611, M, K, 2, "u")
+    B = datagen.operand(datagen.SEED_BASE + 612, N, K, 3, "s")
+    ctx = allocGEMMContext(M, K, N, 2, 3, False, True)
+    try:
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.lhs.importRegular(A1)
+        ctx.rhs.importRegular(B)
+        gemmBitSerial(ctx)
+        assert np.array_equal(ctx.res.reshape(N, M), O.oracle_gemm(A1, B, 2, 3, False, True))
+        ctx.lhs.importRegular(A2)
+        gemmBitSerial(ctx)
+        assert np.array_equal(ctx.res.reshape(N, M), O.oracle_gemm(A2, B, 2, 3, False, True))
+    finally:
+        deallocGEMMContext(ctx)

@@ -28,7 +28,8 @@ def test_tune_records_winner_and_stays_exact(gbs_lib, tmp_path):
         ctx.rhs.importRegular(B)
         best = C.c_int()
         _capi.check(lib.gbs_tune(ctx._h, 3, C.byref(best), None))
-        assert best.value in (_capi.GBS_PIPE_POPC, _capi.GBS_PIPE_BMMA, _capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS)
+        assert best.value in (_capi.GBS_PIPE_POPC, _capi.GBS_PIPE_BMMA, _capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS,
+                              _capi.GBS_PIPE_TC_SMEM)
         assert ctx.pipe == best.value  # AUTO follows the store
         gemmBitSerial(ctx)
         got = ctx.res.reshape(N, M)
@@ -44,7 +45,8 @@ def test_tune_records_winner_and_stays_exact(gbs_lib, tmp_path):
 
 
 CANDIDATES = [(_capi.GBS_PIPE_POPC, v) for v in (-1, 0, 1, 2)] + [(_capi.GBS_PIPE_BMMA, -1)] + \
-    [(_capi.GBS_PIPE_TC, 128), (_capi.GBS_PIPE_TC, 256), (_capi.GBS_PIPE_TC_PAIRS, 128), (_capi.GBS_PIPE_TC_PAIRS, 256)]
+    [(_capi.GBS_PIPE_TC, 128), (_capi.GBS_PIPE_TC, 256), (_capi.GBS_PIPE_TC_SMEM, 128), (_capi.GBS_PIPE_TC_SMEM, 256),
+     (_capi.GBS_PIPE_TC_PAIRS, 128), (_capi.GBS_PIPE_TC_PAIRS, 256)]
 
 
 def test_every_candidate_is_exact(gbs_lib):
