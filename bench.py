@@ -263,6 +263,8 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2):
             "grouped_gops": round(gops_total / (t_group * 1e-3) / 1e9, 1),
             "grouped_tbinops": round(binops / (t_group * 1e-3) / 1e12, 2),
             "tiles": stats["tiles"], "grid": stats["grid"], "smem_bytes": stats["smem_bytes"],
+            "popc_problems": stats["popc_problems"], "tc_problems": stats["tc_problems"],
+            "tc_tiles": stats["tc_tiles"],
             "parity": "grouped == plain (sampled 14 problems)" if ok else "MISMATCH",
             "mix": "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
 

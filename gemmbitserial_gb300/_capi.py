@@ -54,6 +54,7 @@ SIGNATURES = {
     "gbs_group_replay": (i32, [vp, vp]),
     "gbs_group_status": (i32, [vp, vp]),
     "gbs_group_stats": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+    "gbs_group_split": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
     "gbs_group_free": (i32, [vp]),
     "gbs_debug_group_poison_tile": (i32, [vp, C.c_uint32]),
     "gbs_pipe_peaks": (i32, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),

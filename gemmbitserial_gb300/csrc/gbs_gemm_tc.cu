@@ -31,6 +31,7 @@
 #include <cstring>
 
 #include "gbs_internal.h"
+#include "gbs_tc_common.cuh"
 
 namespace gbs {
 
@@ -44,7 +45,6 @@ constexpr int kPkRowB = 16;         // packed bytes per row per plane per stage 
 constexpr int kDecWarps = 12;  // warps 2..13 decode; warps 2..9 also run the epilogue
 constexpr int kThreads = 64 + 32 * kDecWarps;
 constexpr int kPkSlots = 4;
-constexpr uint32_t kWaitLimit = 1u << 20;
 
 // How the planes of one operand become e4m3 operand tiles.  DIGIT mode: one
 // tile whose value is the whole few-bit number (all planes at once, so one
@@ -67,96 +67,10 @@ struct TcArgs {
   uint32_t idesc;
   TcOperand A, B;
 };
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: true when the phase completed; false on abort or timeout.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it) {
-    if (mbar_try(bar, parity)) return true;
-    if (*abort_flag) return false;
-  }
-  *abort_flag = 1;
-  atomicOr(&g_tc_error, 1u);
-  return false;
+  return mbar_wait_err(bar, parity, abort_flag, &g_tc_error);
 }
-// Bounded wait that ignores the abort flag: drains work this thread issued.
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it)
-    if (mbar_try(bar, parity)) return;
-  atomicOr(&g_tc_error, 2u);
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-               : "memory");
-}
-
-// 4 bits -> 4 bytes holding 0 or 1 (bit i -> byte i); the multiply places the
-// bits at 0..3, 7..10, 14..17, 21..24 without carries, the mask keeps 0, 8, 16, 24.
-__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
-
-__device__ __forceinline__ uint32_t bfe4(uint32_t x, int sh) {
-  uint32_t r;
-  asm("bfe.u32 %0, %1, %2, 4;" : "=r"(r) : "r"(x), "r"(sh));
-  return r;
-}
-
-// e4m3 bytes of 4 consecutive columns of one tile row: codes from the tile's
-// planes (bits at column offset `sh` of each plane's 32-bit word), then a
-// byte-permute lookup in the tile's 16-entry table.  Plane p's nibble is
-// spread straight to bit p of each byte (multiplier and mask shifted by p).
-template <int CNT>
-__device__ __forceinline__ uint32_t decode4(const uint32_t (&pw)[4], int sh, const uint32_t (&tab)[4]) {
-  uint32_t c = 0;
-#pragma unroll
-  for (int p = 0; p < CNT; p++) c |= (bfe4(pw[p], sh) * (0x00204081u << p)) & (0x01010101u << p);
-  if (CNT == 1) return c;  // caller maps 0/1 bytes itself
-  const uint32_t t = c | (c >> 4);                        // byte 0 = c0 | c1<<4, byte 2 = c2 | c3<<4
-  const uint32_t sel = __byte_perm(t, 0u, 0x0020u);        // nibbles c0 c1 c2 c3 in the low 16 bits
-  if (CNT <= 3) return __byte_perm(tab[0], tab[1], sel);
-  const uint32_t lo = __byte_perm(tab[0], tab[1], sel & 0x7777u);
-  const uint32_t hi = __byte_perm(tab[2], tab[3], sel & 0x7777u);
-  const uint32_t m = ((c >> 3) & 0x01010101u) * 0xFFu;     // codes 8..15 take the high table
-  return (lo & ~m) | (hi & m);
-}
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) { mbar_drain_err(bar, parity, &g_tc_error); }
 
 // One tile row of one stage: CNT planes (16 bytes each, `pstride` apart) ->
 // 128 e4m3 bytes written as 8 swizzled 16-byte chunks.  Columns at or past
@@ -365,44 +279,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // ---------------------------------------------------------------- HBM digit path
-// Expansion: one thread per 16 columns of one padded row writes the row's
-// e4m3 digits (16 bytes) of operand planes -> digit matrix [nrows_a][ncols_a].
-// Rows past nrows and columns past K are 0, so padding never contributes.
-template <int CNT>
-__global__ void __launch_bounds__(256) expand_digits_kernel(const uint64_t *__restrict__ planes,
-                                                            uint8_t *__restrict__ out, uint64_t nrows,
-                                                            uint64_t nrows_a, uint64_t K, uint64_t ncols_a,
-                                                            uint64_t wpr, uint4 tabv) {
-  const uint64_t chunks = ncols_a / 16;
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nrows_a * chunks) return;
-  const uint64_t r = i / chunks, col0 = (i % chunks) * 16;
-  uint4 res = make_uint4(0u, 0u, 0u, 0u);
-  if (r < nrows && col0 < K) {
-    const uint64_t w = col0 >> 6;
-    const int sh = (int)(col0 & 63);
-    uint32_t pw[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-    for (int p = 0; p < CNT; p++) pw[p] = (uint32_t)(planes[p * nrows_a * wpr + r * wpr + w] >> (sh & 32));
-    const uint32_t tab[4] = {tabv.x, tabv.y, tabv.z, tabv.w};
-    uint32_t q[4];
-#pragma unroll
-    for (int n = 0; n < 4; n++) {
-      const int s4 = (sh & 16) + 4 * n;
-      if (CNT == 1) {
-        const uint32_t sp = decode4<1>(pw, s4, tab);
-        q[n] = sp * ((tab[0] >> 8) & 0xFFu) + (sp ^ 0x01010101u) * (tab[0] & 0xFFu);
-      } else {
-        q[n] = decode4<CNT>(pw, s4, tab);
-      }
-      const uint64_t c0 = col0 + 4 * n;
-      if (c0 + 4 > K) q[n] &= c0 >= K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (K - c0))));
-    }
-    res = make_uint4(q[0], q[1], q[2], q[3]);
-  }
-  *reinterpret_cast<uint4 *>(out + r * ncols_a + col0) = res;
-}
-
 // TMA-fed GEMM on digit matrices: 128 x BN output tile per CTA.
 //   warp 0     TMA: A box 128 rows x 128 bytes, B boxes 128 rows x 128 bytes
 //              (BN/128 of them), 128-byte swizzle = the MMA's K-major layout
@@ -667,6 +543,27 @@ size_t tc_smem(int ntA, int ntB, int wa, int wb, int bn, int no) {
 
 }  // namespace
 
+bool tc_map_u8(void *map, const uint8_t *base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || box_rows == 0 || box_rows > 256) return false;
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols};
+  cuuint32_t box[2] = {128, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void *)base, dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+void tc_digit_table(const Mat &m, uint32_t tab[4]) {
+  const TcOperand op = make_operand(m, true);
+  for (int i = 0; i < 4; i++) tab[i] = op.tab[0][i];
+}
+
+uint64_t tc_max_abs(const Mat &m) { return max_abs(m); }
+
+bool tc_encoder_available() { return encode_fn() != nullptr; }
+
 // The tensor-core pipe applies when every partial sum stays exact in fp32,
 // at most 4 planes per operand and 5 in total fit the operand ring, and
 // both dimensions fill at least half a tile.
@@ -742,24 +639,9 @@ bool make_digit_map(CUtensorMap *map, const uint8_t *digits, const Mat &m) {
 }
 
 cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
-  Mat &m = side ? c->rhs : c->lhs;
-  if (!c->digits[side]) {
-    cudaError_t e = dev_alloc((void **)&c->digits[side], m.nrows_a * m.ncols_a);
-    if (e != cudaSuccess) return e;
-    c->digit_maps_ready = false;
-  }
-  const TcOperand op = make_operand(m, true);
-  const uint4 tab = make_uint4(op.tab[0][0], op.tab[0][1], op.tab[0][2], op.tab[0][3]);
-  const uint64_t threads = m.nrows_a * (m.ncols_a / 16);
-  const unsigned blocks = (unsigned)((threads + 255) / 256);
-  switch (m.nbits) {
-    case 1: expand_digits_kernel<1><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
-    case 2: expand_digits_kernel<2><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
-    case 3: expand_digits_kernel<3><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
-    default: expand_digits_kernel<4><<<blocks, 256, 0, s>>>(m.planes, c->digits[side], m.nrows, m.nrows_a, m.ncols, m.ncols_a, m.wpr(), tab); break;
-  }
-  count_launch();
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = ensure_digit_buffer(c, side);
+  if (e != cudaSuccess) return e;
+  e = launch_expand(make_expand_job(side ? c->rhs : c->lhs, c->digits[side]), s);
   if (e == cudaSuccess) c->digits_valid[side] = true;
   return e;
 }

@@ -9,7 +9,14 @@
 //     atomic counter over a tile table sorted by decreasing cost),
 // and can capture that sequence once into a CUDA graph for replay.  Each
 // problem keeps its own context, so results land in each context's res.
+//
+// Problems go to one of two persistent kernels: the tensor-core kernel over
+// e4m3 digit matrices (gbs_gemm_tcg.cu) where it is exact and cheaper, the
+// CUDA-core popcount kernel otherwise.  GBS_GROUP_PIPE=popc or =tc in the
+// environment forces one kernel (tc: wherever it is exact).  Digit matrices
+// are rebuilt by one grouped expansion launch after every import.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -22,7 +29,7 @@ struct gbs_group {
   gbs::GroupProblem *d_probs = nullptr;
   gbs::GroupTile *d_tiles = nullptr;
   uint32_t ntiles = 0;
-  uint32_t *d_scratch = nullptr;  // [0] tile counter, [1] error bits
+  uint32_t *d_scratch = nullptr;  // [0] tile counter, [1] popcount-kernel error bits, [2] tensor-core error bits
   gbs::PackJob *d_rs_jobs = nullptr;
   int nrs = 0;
   uint64_t rs_warps = 0;
@@ -33,6 +40,9 @@ struct gbs_group {
   int grid = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  gbs::TcgPlan tc;  // problems on the tensor-core kernel
+  uint64_t launches_per_replay = 0;
+  uint32_t popc_tiles = 0;
 };
 
 namespace gbs {
@@ -51,6 +61,7 @@ bool device_ptr(const void *p) {
 }
 
 void free_group(gbs_group *g) {
+  tcg_plan_free(&g->tc);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   if (g->d_probs) cudaFree(g->d_probs);
@@ -111,12 +122,32 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
 }
 
 cudaError_t enqueue_gemm(gbs_group *g, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(g->d_scratch, 0, sizeof(uint32_t), s);  // tile counter only
-  if (e == cudaSuccess && g->nrs) e = launch_rowsum_grouped(g->d_rs_jobs, g->nrs, g->rs_warps, s);
-  if (e == cudaSuccess && g->ntiles)
-    e = launch_gemm_popc_grouped(g->d_probs, (int)g->ctxs.size(), g->d_tiles, g->ntiles, g->d_scratch,
-                                 g->d_scratch + 1, g->smem, g->grid, s);
+  cudaError_t e = cudaSuccess;
+  if (g->popc_tiles) {
+    e = cudaMemsetAsync(g->d_scratch, 0, sizeof(uint32_t), s);  // tile counter only
+    if (e == cudaSuccess && g->nrs) e = launch_rowsum_grouped(g->d_rs_jobs, g->nrs, g->rs_warps, s);
+    if (e == cudaSuccess)
+      e = launch_gemm_popc_grouped(g->d_probs, (int)g->ctxs.size(), g->d_tiles, g->popc_tiles, g->d_scratch,
+                                   g->d_scratch + 1, g->smem, g->grid, s);
+  }
+  if (e == cudaSuccess) e = tcg_gemm(g->tc, g->d_scratch + 2, s);
   return e;
+}
+
+// True when some tensor-core problem's digit matrices are older than its planes.
+bool digits_stale(const gbs_group *g) {
+  for (const gbs_ctx *c : g->tc.ctxs)
+    if (!c->digits_valid[0] || !c->digits_valid[1]) return true;
+  return false;
+}
+
+// 0 = per-problem choice, 1 = popcount kernel only, 2 = tensor-core kernel wherever exact.
+int group_pipe_mode() {
+  const char *v = getenv("GBS_GROUP_PIPE");
+  if (!v) return 0;
+  if (!strcmp(v, "popc")) return 1;
+  if (!strcmp(v, "tc")) return 2;
+  return 0;
 }
 
 }  // namespace
@@ -141,6 +172,8 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
   std::vector<PackJob> rs;
   uint64_t rs_warps = 0;
   size_t smem = 16;
+  const int mode = group_pipe_mode();
+  std::vector<gbs_ctx *> tc_ctxs;
   for (int p = 0; p < count; p++) {
     gbs_ctx *c = ctxs[p];
     if (!c) {
@@ -152,6 +185,13 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
       return fail(GBS_EINVAL, "gbs_group_create: contexts must live on the current device");
     }
     g->ctxs.push_back(c);
+    if (mode != 1 && tcg_eligible(c) && (mode == 2 || tcg_preferred(c))) {
+      tc_ctxs.push_back(c);
+      GroupProblem none;  // keeps the popcount table indexed by problem
+      memset(&none, 0, sizeof(none));
+      probs.push_back(none);
+      continue;
+    }
     Epilogue e;
     make_epilogue(c, e, c->rowsum);
     GroupProblem P;
@@ -209,24 +249,32 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
   std::vector<GroupTile> sorted(tiles.size());
   for (size_t i = 0; i < order.size(); i++) sorted[i] = tiles[order[i]];
 
+  if (!tc_ctxs.empty()) {
+    const int rc = tcg_plan_build(&g->tc, tc_ctxs.data(), (int)tc_ctxs.size());
+    if (rc != GBS_OK) {
+      free_group(g);
+      return rc;
+    }
+  }
   cudaError_t e = upload(&g->d_probs, probs);
   if (e == cudaSuccess) e = upload(&g->d_tiles, sorted);
   if (e == cudaSuccess) e = upload(&g->d_rs_jobs, rs);
-  if (e == cudaSuccess) e = dev_alloc((void **)&g->d_scratch, 2 * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMemset(g->d_scratch, 0, 2 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = dev_alloc((void **)&g->d_scratch, 3 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(g->d_scratch, 0, 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = prepare_gemm_popc_grouped(smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     free_group(g);
     return fail(GBS_ENOMEM, "gbs_group_create: device allocation or upload failed");
   }
-  g->ntiles = (uint32_t)sorted.size();
+  g->popc_tiles = (uint32_t)sorted.size();
+  g->ntiles = g->popc_tiles + g->tc.ntiles;
   g->nrs = (int)rs.size();
   g->rs_warps = rs_warps;
   g->smem = smem;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, g->device);
-  g->grid = std::max(1, std::min<int>((int)g->ntiles, sms * grouped_blocks_per_sm(smem)));
+  g->grid = std::max(1, std::min<int>((int)g->popc_tiles, sms * grouped_blocks_per_sm(smem)));
   *out = g;
   return GBS_OK;
 }
@@ -246,6 +294,8 @@ int gbs_group_import(gbs_group *g, const void *const *lhs_srcs, const void *cons
   cudaError_t e = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_import: pack kernel");
   for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
+  e = tcg_expand(g->tc, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_import: digit expansion");
   return GBS_OK;
 }
 
@@ -253,7 +303,9 @@ int gbs_group_gemm(gbs_group *g, void *stream) {
   if (!g) return fail(GBS_EINVAL, "gbs_group_gemm: group is NULL");
   for (gbs_ctx *c : g->ctxs)
     if (!c->lhs.imported || !c->rhs.imported) return fail(GBS_ESTATE, "gbs_group_gemm: import every operand first");
-  cudaError_t e = enqueue_gemm(g, (cudaStream_t)stream);
+  cudaError_t e = cudaSuccess;
+  if (digits_stale(g)) e = tcg_expand(g->tc, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = enqueue_gemm(g, (cudaStream_t)stream);
   return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_group_gemm");
 }
 
@@ -274,16 +326,23 @@ int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *con
   g->exec = nullptr;
   g->graph = nullptr;
   cudaStream_t s = (cudaStream_t)stream;
+  if (!with_pack && digits_stale(g)) {  // the graph then holds the GEMMs only
+    cudaError_t xe = tcg_expand(g->tc, s);
+    if (xe != cudaSuccess) return cuda_fail(xe, "gbs_group_capture: digit expansion");
+  }
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: begin capture");
   cudaError_t ke = cudaSuccess;
   if (with_pack) ke = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, s);
+  if (ke == cudaSuccess && with_pack) ke = tcg_expand(g->tc, s);
   if (ke == cudaSuccess) ke = enqueue_gemm(g, s);
   e = cudaStreamEndCapture(s, &g->graph);
   if (ke != cudaSuccess) return cuda_fail(ke, "gbs_group_capture: enqueue");
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: end capture");
   e = cudaGraphInstantiate(&g->exec, g->graph, 0);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: instantiate");
+  g->launches_per_replay = (with_pack && g->npack ? 1 : 0) + (with_pack && g->tc.njobs ? 1 : 0) +
+                           (g->popc_tiles ? 1 + (g->nrs ? 1 : 0) : 0) + (g->tc.ntiles ? 1 : 0);
   if (with_pack)
     for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
   return GBS_OK;
@@ -293,18 +352,21 @@ int gbs_group_replay(gbs_group *g, void *stream) {
   if (!g || !g->exec) return fail(GBS_ESTATE, "gbs_group_replay: capture the group first");
   cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_replay");
-  count_launch((g->npack ? 1 : 0) + (g->nrs ? 1 : 0) + 1);
+  count_launch(g->launches_per_replay);
   return GBS_OK;
 }
 
 int gbs_group_status(gbs_group *g, void *stream) {
   if (!g) return fail(GBS_EINVAL, "gbs_group_status: group is NULL");
-  uint32_t err = 0;
-  cudaError_t e = cudaMemcpyAsync(&err, g->d_scratch + 1, sizeof(err), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  uint32_t err[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(err, g->d_scratch + 1, sizeof(err), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_status");
-  if (err) return fail(GBS_EINVAL, "gbs_group_status: the grouped kernel rejected tile descriptors (bits " +
-                                       std::to_string(err) + ")");
+  if (err[0]) return fail(GBS_EINVAL, "gbs_group_status: the grouped kernel rejected tile descriptors (bits " +
+                                          std::to_string(err[0]) + ")");
+  if (err[1] & 4u) return fail(GBS_EINVAL, "gbs_group_status: the tensor-core kernel rejected tile descriptors");
+  if (err[1]) return fail(GBS_ECUDA, "gbs_group_status: a tensor-core pipeline wait timed out (bits " +
+                                         std::to_string(err[1]) + ")");
   return GBS_OK;
 }
 
@@ -316,10 +378,24 @@ int gbs_group_stats(const gbs_group *g, uint64_t *ntiles, uint64_t *smem_bytes, 
   return GBS_OK;
 }
 
+int gbs_group_split(const gbs_group *g, uint64_t *popc_problems, uint64_t *tc_problems, uint64_t *tc_tiles) {
+  if (!g) return fail(GBS_EINVAL, "gbs_group_split: group is NULL");
+  if (popc_problems) *popc_problems = g->ctxs.size() - g->tc.ctxs.size();
+  if (tc_problems) *tc_problems = g->tc.ctxs.size();
+  if (tc_tiles) *tc_tiles = g->tc.ntiles;
+  return GBS_OK;
+}
+
 int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile) {
   if (!g || tile >= g->ntiles) return fail(GBS_EINVAL, "gbs_debug_group_poison_tile: bad tile");
-  GroupTile bad{0xffffffffu, 0u, 0u, 0u};
-  cudaError_t e = cudaMemcpy(g->d_tiles + tile, &bad, sizeof(bad), cudaMemcpyHostToDevice);
+  cudaError_t e;
+  if (tile < g->popc_tiles) {
+    GroupTile bad{0xffffffffu, 0u, 0u, 0u};
+    e = cudaMemcpy(g->d_tiles + tile, &bad, sizeof(bad), cudaMemcpyHostToDevice);
+  } else {
+    TcgTile bad{0xffffffffu, 0u, 0u, 0u};
+    e = cudaMemcpy(g->tc.d_tiles + (tile - g->popc_tiles), &bad, sizeof(bad), cudaMemcpyHostToDevice);
+  }
   return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_debug_group_poison_tile");
 }
 

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/gbs.h"
 
@@ -72,6 +73,47 @@ struct PackJob {
   int32_t *rowsum;
   uint64_t nrows, ncols, nrows_a, wpr, warp0;
   int nbits, issigned, dtype, vec;
+};
+
+// One problem of the persistent tensor-core kernel (device resident).  The
+// MMA's row operand ("MMA-A", 128 rows per tile) is the lhs, or the rhs when
+// swap is set; the other operand gives the MMA's N = bn columns per tile.
+struct TcgProblem {
+  int32_t *C;               // result [N][M]
+  uint32_t M, N;
+  uint32_t a_rows, b_rows;  // padded rows of the MMA-A / MMA-B digit matrices
+  uint32_t nk;              // K stages of 128 digits
+  uint32_t bn;              // MMA N: a multiple of 16 in [16, 256]
+  uint32_t idesc;           // tcgen05 instruction descriptor for M = 128, N = bn
+  uint32_t swap;            // 1: MMA-A = rhs (tile rows are n), MMA-B = lhs (columns are m)
+};
+
+// One output tile: problem, 128-row block of MMA-A, bn-column block of MMA-B.
+struct TcgTile {
+  uint32_t p, r, c, pad;
+};
+
+// One operand of a digit expansion pass (planes -> e4m3 digit matrix).
+struct ExpandJob {
+  const uint64_t *planes;
+  uint8_t *digits;
+  uint64_t nrows_a, wpr, ncols_a;
+  uint64_t thread0;  // first global thread of this job (16 digits per thread)
+  uint32_t nrows, K, chunks, nbits;
+  uint32_t tab[4];   // e4m3 byte of every plane code, 4 per word
+};
+
+// Host-side plan of the persistent tensor-core kernel over some contexts.
+struct TcgPlan {
+  std::vector<gbs_ctx *> ctxs;
+  TcgProblem *d_probs = nullptr;
+  void *d_maps = nullptr;  // CUtensorMap [2 * nprob]: MMA-A map, MMA-B map of each problem
+  TcgTile *d_tiles = nullptr;
+  ExpandJob *d_jobs = nullptr;
+  uint32_t nprob = 0, ntiles = 0;
+  int njobs = 0;
+  uint64_t expand_threads = 0;
+  int grid = 0;
 };
 
 struct GemmShape {
@@ -144,6 +186,23 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
+
+// tensor-map and digit helpers shared by the tensor-core files (gbs_gemm_tc.cu)
+bool tc_map_u8(void *map, const uint8_t *base, uint64_t cols, uint64_t rows, uint32_t box_rows);
+void tc_digit_table(const Mat &m, uint32_t tab[4]);
+uint64_t tc_max_abs(const Mat &m);
+bool tc_encoder_available();
+
+// persistent tensor-core kernel over a table of problems (gbs_gemm_tcg.cu)
+bool tcg_eligible(const gbs_ctx *c);
+bool tcg_preferred(const gbs_ctx *c);
+int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n);
+void tcg_plan_free(TcgPlan *plan);
+cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s);
+cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s);
+cudaError_t ensure_digit_buffer(gbs_ctx *c, int side);
+ExpandJob make_expand_job(const Mat &m, uint8_t *digits);
+cudaError_t launch_expand(const ExpandJob &job, cudaStream_t s);
 int effective_pipe(const gbs_ctx *c);
 int tuned_variant(const gbs_ctx *c, int pipe);
 

@@ -1,0 +1,109 @@
+// gbs_tc_common.cuh -- device primitives shared by the tensor-core kernels:
+// mbarriers with bounded waits, TMA tile loads, tcgen05 descriptors and MMA
+// issue, and the bit-plane -> e4m3 digit decode.
+#pragma once
+#include <cuda.h>
+#include <stdint.h>
+
+namespace gbs {
+
+// Iterations of mbarrier try_wait before a wait gives up (each try_wait may
+// also suspend the thread for a short, hardware-chosen time).
+constexpr uint32_t kTcWaitLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n selp.b32 %0, 1, 0, P;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: true when the phase completed; false on abort or timeout.
+// A timeout raises the CTA's abort flag and sets bit 0 of *err.
+__device__ __forceinline__ bool mbar_wait_err(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                              uint32_t *err) {
+  for (uint32_t it = 0; it < kTcWaitLimit; ++it) {
+    if (mbar_try(bar, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  atomicOr(err, 1u);
+  return false;
+}
+// Bounded wait that ignores the abort flag: drains work this thread issued.
+// A timeout sets bit 1 of *err.
+__device__ __forceinline__ void mbar_drain_err(uint32_t bar, uint32_t parity, uint32_t *err) {
+  for (uint32_t it = 0; it < kTcWaitLimit; ++it)
+    if (mbar_try(bar, parity)) return;
+  atomicOr(err, 2u);
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_f8(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+// 4 bits -> 4 bytes holding 0 or 1 (bit i -> byte i); the multiply places the
+// bits at 0..3, 7..10, 14..17, 21..24 without carries, the mask keeps 0, 8, 16, 24.
+__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
+
+__device__ __forceinline__ uint32_t bfe4(uint32_t x, int sh) {
+  uint32_t r;
+  asm("bfe.u32 %0, %1, %2, 4;" : "=r"(r) : "r"(x), "r"(sh));
+  return r;
+}
+
+// e4m3 bytes of 4 consecutive columns of one tile row: codes from the tile's
+// planes (bits at column offset `sh` of each plane's 32-bit word), then a
+// byte-permute lookup in the tile's 16-entry table.  Plane p's nibble is
+// spread straight to bit p of each byte (multiplier and mask shifted by p).
+template <int CNT>
+__device__ __forceinline__ uint32_t decode4(const uint32_t (&pw)[4], int sh, const uint32_t (&tab)[4]) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int p = 0; p < CNT; p++) c |= (bfe4(pw[p], sh) * (0x00204081u << p)) & (0x01010101u << p);
+  if (CNT == 1) return c;  // caller maps 0/1 bytes itself
+  const uint32_t t = c | (c >> 4);                        // byte 0 = c0 | c1<<4, byte 2 = c2 | c3<<4
+  const uint32_t sel = __byte_perm(t, 0u, 0x0020u);        // nibbles c0 c1 c2 c3 in the low 16 bits
+  if (CNT <= 3) return __byte_perm(tab[0], tab[1], sel);
+  const uint32_t lo = __byte_perm(tab[0], tab[1], sel & 0x7777u);
+  const uint32_t hi = __byte_perm(tab[2], tab[3], sel & 0x7777u);
+  const uint32_t m = ((c >> 3) & 0x01010101u) * 0xFFu;     // codes 8..15 take the high table
+  return (lo & ~m) | (hi & m);
+}
+
+
+}  // namespace gbs

@@ -62,7 +62,10 @@ class Group:
     def stats(self):
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _capi.check(_capi.load().gbs_group_stats(self._h, C.byref(a), C.byref(b), C.byref(c)))
-        return {"tiles": a.value, "smem_bytes": b.value, "grid": c.value}
+        d, e, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _capi.check(_capi.load().gbs_group_split(self._h, C.byref(d), C.byref(e), C.byref(f)))
+        return {"tiles": a.value, "smem_bytes": b.value, "grid": c.value,
+                "popc_problems": d.value, "tc_problems": e.value, "tc_tiles": f.value}
 
     def free(self):
         if self._h:

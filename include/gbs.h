@@ -217,8 +217,17 @@ GBS_API int gbs_group_replay(gbs_group *g, void *stream);
  * GBS_EINVAL if the grouped kernel rejected a tile descriptor. */
 GBS_API int gbs_group_status(gbs_group *g, void *stream);
 
-/* Tile count, dynamic shared memory per CTA and persistent grid size. */
+/* Tile count (both kernels), and dynamic shared memory per CTA and
+ * persistent grid size of the CUDA-core popcount kernel. */
 GBS_API int gbs_group_stats(const gbs_group *g, uint64_t *ntiles, uint64_t *smem_bytes, uint64_t *grid);
+
+/* How the group's problems are split between the CUDA-core popcount kernel
+ * and the tensor-core kernel over e4m3 digit matrices, and the tensor-core
+ * kernel's tile count.  The tensor-core kernel takes a problem when its
+ * result is exact in fp32 (K * max|a| * max|b| < 2^24, at most 4 bits per
+ * operand) and it is the cheaper one; GBS_GROUP_PIPE=popc or =tc in the
+ * environment at gbs_group_create forces one kernel. */
+GBS_API int gbs_group_split(const gbs_group *g, uint64_t *popc_problems, uint64_t *tc_problems, uint64_t *tc_tiles);
 
 /* Synchronises the device and frees the group (not its contexts). */
 GBS_API int gbs_group_free(gbs_group *g);

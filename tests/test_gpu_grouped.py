@@ -24,7 +24,27 @@ def make_contexts(mix):
     return [allocGEMMContext(M, K, N, wA, wB, eA != "u", eB != "u") for (M, K, N, wA, eA, wB, eB) in mix]
 
 
-def test_grouped_reduced_mix_matches_oracle():
+@pytest.fixture(params=["auto", "tc", "popc"])
+def group_pipe(request, monkeypatch):
+    """GBS_GROUP_PIPE as read by gbs_group_create: per-problem choice, or one kernel forced."""
+    if request.param == "auto":
+        monkeypatch.delenv("GBS_GROUP_PIPE", raising=False)
+    else:
+        monkeypatch.setenv("GBS_GROUP_PIPE", request.param)
+    return request.param
+
+
+def check_split(g, mode, count):
+    st = g.stats()
+    assert st["popc_problems"] + st["tc_problems"] == count
+    if mode == "popc":
+        assert st["tc_problems"] == 0
+    if mode == "tc":
+        assert st["tc_problems"] > 0
+    return st
+
+
+def test_grouped_reduced_mix_matches_oracle(group_pipe):
     import torch
     mix = datagen.grouped_mix(seed=datagen.SEED_BASE + 77, count=96, k_words=(1, 40), n_range=(1, 700))
     host = []
@@ -41,6 +61,7 @@ def test_grouped_reduced_mix_matches_oracle():
     s = torch.cuda.Stream()
     g = Group(ctxs)
     try:
+        check_split(g, group_pipe, len(mix))
         with torch.cuda.stream(s):
             g.import_([a for a, _ in dev], [b for _, b in dev], stream=s)
             g.gemm(stream=s)
@@ -58,6 +79,56 @@ def test_grouped_reduced_mix_matches_oracle():
         for (M, K, N, wA, eA, wB, eB), (A, B), c in zip(mix, host, ctxs):
             want = O.oracle_gemm(A, B, wA, wB, eA != "u", eB != "u")
             assert np.array_equal(c.res.reshape(N, M), want)
+    finally:
+        g.free()
+        for c in ctxs:
+            deallocGEMMContext(c)
+
+
+# Tile geometry of the tensor-core kernel: lhs-major and rhs-major problems,
+# MMA N from 16 to 256, several column tiles, M not a multiple of 4, 1-row
+# operands, K not a multiple of 128, every encoding pair, and the largest K
+# whose sums stay exact in fp32 for 4 x 4-bit unsigned operands.
+EDGE_MIX = [
+    (300, 640, 70, 2, "u", 3, "s"),      # M > N: lhs is the MMA row operand
+    (520, 1000, 600, 1, "b", 2, "u"),    # M < N, both > 256: 3 column tiles of 256
+    (17, 333, 129, 4, "s", 1, "b"),      # M odd: scalar stores of result rows
+    (1, 64, 1, 1, "u", 1, "u"),
+    (1, 4096, 3000, 4, "u", 4, "s"),
+    (256, 192, 256, 1, "b", 1, "b"),
+    (128, 2048, 128, 3, "u", 3, "u"),
+    (64, 74565, 96, 4, "u", 4, "u"),     # 74565 * 15 * 15 < 2^24
+    (96, 512, 48, 2, "s", 4, "s"),
+    (200, 129, 1, 2, "u", 2, "u"),
+]
+
+
+def test_grouped_tc_edge_shapes(group_pipe):
+    import torch
+    host = [(datagen.operand(datagen.SEED_BASE + 3000 + 2 * i, M, K, wA, eA),
+             datagen.operand(datagen.SEED_BASE + 3001 + 2 * i, N, K, wB, eB))
+            for i, (M, K, N, wA, eA, wB, eB) in enumerate(EDGE_MIX)]
+    ctxs = make_contexts(EDGE_MIX)
+    dev = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in host]
+    g = Group(ctxs)
+    try:
+        st = check_split(g, group_pipe, len(EDGE_MIX))
+        if group_pipe == "tc":
+            assert st["tc_problems"] == len(EDGE_MIX)
+        g.import_([a for a, _ in dev], [b for _, b in dev])
+        g.gemm()
+        torch.cuda.synchronize()
+        assert g.status() == _capi.GBS_OK
+        for (M, K, N, wA, eA, wB, eB), (A, B), c in zip(EDGE_MIX, host, ctxs):
+            want = O.oracle_gemm(A, B, wA, wB, eA != "u", eB != "u", threads=8)
+            assert np.array_equal(c.res.reshape(N, M), want), (M, K, N, wA, eA, wB, eB)
+        # re-importing one context alone makes its digits stale; the group rebuilds them
+        A2 = datagen.operand(datagen.SEED_BASE + 3999, 300, 640, 2, "u")
+        ctxs[0].lhs.importRegular(torch.from_numpy(A2).cuda())
+        g.gemm()
+        torch.cuda.synchronize()
+        want = O.oracle_gemm(A2, host[0][1], 2, 3, False, True)
+        assert np.array_equal(ctxs[0].res.reshape(70, 300), want)
     finally:
         g.free()
         for c in ctxs:
