@@ -6,6 +6,7 @@
 // arch-generic.hpp:331-345) with its encoding-dependent epilogue
 // (prepareAccumulators_generic, :39-76; usingBinary weights, :179-192;
 // bipolar correction, :255-259), result read-back and deallocation.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -79,7 +80,13 @@ void free_ctx_buffers(gbs_ctx *c) {
   if (c->rhs.planes) cudaFree(c->rhs.planes);
   if (c->res) cudaFree(c->res);
   if (c->rowsum) cudaFree(c->rowsum);
-  if (c->stage) cudaFree(c->stage);
+  for (int side = 0; side < 2; side++) {
+    if (c->stage[side]) cudaFree(c->stage[side]);
+    if (c->ev_packed[side]) cudaEventDestroy(c->ev_packed[side]);
+  }
+  for (cudaEvent_t ev : c->ev_chunk)
+    if (ev) cudaEventDestroy(ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->digits[0]) cudaFree(c->digits[0]);
   if (c->digits[1]) cudaFree(c->digits[1]);
 }
@@ -230,6 +237,45 @@ int gbs_ctx_get_info(const gbs_ctx *c, gbs_ctx_info *info) {
   return GBS_OK;
 }
 
+namespace {
+
+constexpr int kImportChunks = 8;            // at most this many copy/pack chunks per host import
+constexpr size_t kImportChunkBytes = 2 << 20;
+
+// Copy stream and events of host-source imports, created on first use.
+cudaError_t ensure_import_streams(gbs_ctx *c) {
+  if (c->copy_stream) return cudaSuccess;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < kImportChunks && e == cudaSuccess; i++)
+    e = cudaEventCreateWithFlags(&c->ev_chunk[i], cudaEventDisableTiming);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&c->ev_packed[i], cudaEventDisableTiming);
+  return e;
+}
+
+// Staging buffer of one side holding at least `bytes`.  A buffer that grows
+// is freed only after the packing that reads it has finished.
+int ensure_stage(gbs_ctx *c, int side, size_t bytes, cudaStream_t s) {
+  if (c->stage_bytes[side] >= bytes) return GBS_OK;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && c->ev_packed_set[side]) e = cudaEventSynchronize(c->ev_packed[side]);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_import: stream sync");
+  if (c->stage[side]) cudaFree(c->stage[side]);
+  c->stage[side] = nullptr;
+  c->stage_bytes[side] = 0;
+  if (dev_alloc(&c->stage[side], bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GBS_ENOMEM, "gbs_import: staging allocation failed");
+  }
+  c->stage_bytes[side] = bytes;
+  return GBS_OK;
+}
+
+// The tensor-core digit pipe will run this context's GEMM: the import then
+// writes the digit matrix too, so the GEMM needs no expansion pass.
+bool import_writes_digits(const gbs_ctx *c) { return effective_pipe(c) == GBS_PIPE_TC; }
+
+}  // namespace
+
 int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, void *stream) {
   if (!c) return fail(GBS_EINVAL, "gbs_import: ctx is NULL");
   if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_import: side must be 0 (lhs) or 1 (rhs)");
@@ -240,42 +286,80 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
   DeviceGuard g(c->device);
   if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_import: cudaSetDevice");
   cudaStream_t s = as_stream(stream);
-  const void *dsrc = src;
-  if (n && !is_device_ptr(src)) {
-    const size_t bytes = n * elem_size(dtype);
-    if (c->stage_bytes < bytes) {
-      cudaError_t se = cudaStreamSynchronize(s);  // the old staging buffer may still be read
-      if (se != cudaSuccess) return cuda_fail(se, "gbs_import: stream sync");
-      if (c->stage) cudaFree(c->stage);
-      c->stage = nullptr;
-      c->stage_bytes = 0;
-      if (dev_alloc(&c->stage, bytes) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(GBS_ENOMEM, "gbs_import: staging allocation failed");
-      }
-      c->stage_bytes = bytes;
+  c->digits_valid[side] = false;
+  uint8_t *digits = nullptr;
+  uint32_t dtab[4] = {0, 0, 0, 0};
+  if (!col_major && import_writes_digits(c)) {
+    if (ensure_digit_buffer(c, side) == cudaSuccess) {
+      digits = c->digits[side];
+      tc_digit_table(m, dtab);
+    } else {
+      cudaGetLastError();  // the GEMM expands the digits itself
     }
-    cudaError_t ce = cudaMemcpyAsync(c->stage, src, bytes, cudaMemcpyHostToDevice, s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "gbs_import: host-to-device copy");
-    dsrc = c->stage;
-    cudaError_t pe = launch_pack(m, dsrc, dtype, col_major, s);
-    if (pe != cudaSuccess) return cuda_fail(pe, "gbs_import: pack kernel");
-    // Host memory may be reused once the copy has been consumed.
-    ce = cudaStreamSynchronize(s);
-    if (ce != cudaSuccess) return cuda_fail(ce, "gbs_import: stream sync");
+  }
+  cudaError_t e = cudaSuccess;
+  if (n && !is_device_ptr(src)) {
+    const size_t esz = elem_size(dtype), bytes = n * esz;
+    int rc = ensure_stage(c, side, bytes, s);
+    if (rc != GBS_OK) return rc;
+    e = ensure_import_streams(c);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: stream/event creation");
+    // the copy overwrites the staging buffer only after the last packing that read it
+    if (c->ev_packed_set[side]) e = cudaStreamWaitEvent(c->copy_stream, c->ev_packed[side], 0);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: stream wait");
+    if (col_major) {  // one copy, then the column-major pack
+      e = cudaMemcpyAsync(c->stage[side], src, bytes, cudaMemcpyHostToDevice, c->copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(c->ev_chunk[0], c->copy_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_chunk[0], 0);
+      if (e != cudaSuccess) return cuda_fail(e, "gbs_import: host-to-device copy");
+      e = launch_pack(m, c->stage[side], dtype, 1, s);
+      if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack kernel");
+    } else {  // row chunks: the pack of chunk i overlaps the copy of chunk i+1
+      const size_t row_bytes = m.ncols * esz;
+      const uint64_t chunks = std::max<uint64_t>(1, std::min<uint64_t>(kImportChunks, bytes / kImportChunkBytes));
+      const uint64_t rows_per = (m.nrows + chunks - 1) / chunks;
+      int last = 0;
+      for (uint64_t i = 0; i < chunks; i++) {
+        const uint64_t r0 = i * rows_per, r1 = std::min(m.nrows, r0 + rows_per);
+        if (r0 >= r1) break;
+        const size_t off = r0 * row_bytes;
+        e = cudaMemcpyAsync((char *)c->stage[side] + off, (const char *)src + off, (r1 - r0) * row_bytes,
+                            cudaMemcpyHostToDevice, c->copy_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_chunk[i], c->copy_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c->ev_chunk[i], 0);
+        if (e != cudaSuccess) return cuda_fail(e, "gbs_import: host-to-device copy");
+        // the last chunk also writes the zero padding rows [nrows, nrows_a)
+        e = launch_pack_rows(m, c->stage[side], dtype, r0, r1 == m.nrows ? m.nrows_a : r1, digits, dtab, s);
+        if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack kernel");
+        last = (int)i;
+      }
+      if (digits) c->digits_valid[side] = true;
+      e = cudaEventSynchronize(c->ev_chunk[last]);  // host memory may be reused once copied
+      if (e != cudaSuccess) return cuda_fail(e, "gbs_import: copy wait");
+    }
+    e = cudaEventRecord(c->ev_packed[side], s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: event record");
+    c->ev_packed_set[side] = true;
+    if (col_major) {
+      e = cudaEventSynchronize(c->ev_chunk[0]);
+      if (e != cudaSuccess) return cuda_fail(e, "gbs_import: copy wait");
+    }
+  } else if (!col_major) {
+    e = launch_pack_rows(m, src, dtype, 0, m.nrows_a, digits, dtab, s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack kernel");
+    if (digits) c->digits_valid[side] = true;
   } else {
-    cudaError_t pe = launch_pack(m, dsrc, dtype, col_major, s);
-    if (pe != cudaSuccess) return cuda_fail(pe, "gbs_import: pack kernel");
+    e = launch_pack(m, src, dtype, 1, s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack kernel");
   }
   m.imported = true;
-  c->digits_valid[side] = false;  // the digit matrix of this side is rebuilt from the new planes
   return GBS_OK;
 }
 
 int gbs_set_variant(gbs_ctx *c, int variant) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_variant: ctx is NULL");
-  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256))
-    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128 or 256");
+  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256 || variant == kPairVariant))
+    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128, 256 or 512");
   c->variant = variant;
   return GBS_OK;
 }
@@ -297,9 +381,11 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   cudaStream_t s = as_stream(stream);
   const uint64_t M = c->lhs.nrows, N = c->rhs.nrows;
   if (M == 0 || N == 0) return GBS_OK;
+  const int pipe = effective_pipe(c);
+  const bool tensor_core = pipe == GBS_PIPE_TC || pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM;
   Epilogue e;
   make_epilogue(c, e, c->rowsum);
-  if (e.ra || e.rb) {
+  if ((e.ra || e.rb) && !tensor_core) {  // the tensor-core pipes take bipolar values directly
     const Mat &reg = c->lhs.bipolar() ? c->rhs : c->lhs;
     cudaError_t re = launch_rowsum(reg, c->rowsum, s);
     if (re != cudaSuccess) return cuda_fail(re, "gbs_gemm: row-sum kernel");
@@ -317,9 +403,8 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.b_rows = c->rhs.nrows_a;
   sh.wa = (int)c->lhs.nbits;
   sh.wb = (int)c->rhs.nbits;
-  const int pipe = effective_pipe(c);
   const int variant = c->variant >= 0 ? c->variant : (c->pipe == GBS_PIPE_AUTO ? tuned_variant(c, pipe) : -1);
-  sh.tile_cls = (pipe == GBS_PIPE_POPC) ? variant : -1;
+  sh.tile_cls = (pipe == GBS_PIPE_POPC && variant >= 0 && variant <= 2) ? variant : -1;
   cudaError_t ke;
   if (pipe == GBS_PIPE_TC) {
     ke = launch_gemm_tc_hbm(c, s, variant);

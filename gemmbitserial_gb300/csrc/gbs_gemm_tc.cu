@@ -404,6 +404,181 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
   }
 }
 
+// Pair kernel: a cluster of two CTAs on two SMs computes one 256 x 256
+// output tile with tcgen05.mma.cta_group::2 (M = 256, N = 256, K = 32).
+// CTA rank r holds A rows [m0 + 128r, +128) and B rows [n0 + 128r, +128) of
+// every stage and accumulates its 128 result rows x 256 columns in its own
+// TMEM, so each SM receives 32 KB per 128-digit stage for the math a 1-SM
+// 128 x 256 tile does with 48 KB.
+//   warp 0     TMA of this CTA's halves; both CTAs signal the full barrier of
+//              rank 0 (the leader), which expects the bytes of both
+//   warp 1     TMEM allocation (both CTAs, collectively); in the leader, lane
+//              0 issues the MMAs and commits to the empty / accumulator
+//              barriers of both CTAs (multicast)
+//   warps 2-5  epilogue of this CTA's 128 rows
+// A cluster barrier closes the kernel, so no CTA frees TMEM or exits while
+// its peer may still signal its barriers or write its accumulator.
+constexpr int kPairStagesMax = 6;
+constexpr int kPairThreads = 192;
+constexpr uint32_t kPairHalfBytes = 128 * kRowB;  // 128 rows x 128 digits
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t smem_addr, uint32_t rank) {
+  uint32_t d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(smem_addr), "r"(rank));
+  return d;
+}
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
+      "%3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {  // arrives on `bar` in both CTAs
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+      "h"((uint16_t)3)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kPairThreads, 1)
+    gemm_tc_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TmaArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t rank = cluster_rank();
+  const uint32_t stage_bytes = 2 * kPairHalfBytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.stages * stage_bytes);
+  const uint32_t full = smem_u32(bars), empty = full + 8 * a.stages, acc_full = empty + 8 * a.stages;
+  const uint32_t mma_done = acc_full + 8;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * a.stages + 2);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const uint64_t pair_m0 = (uint64_t)(blockIdx.x >> 1) * 256, n0 = (uint64_t)blockIdx.y * 256;
+  const uint64_t m0 = pair_m0 + 128 * rank;
+
+  if (tid == 0) {
+    for (int i = 0; i < a.stages; i++) {
+      mbar_init(full + 8 * i, 1);
+      mbar_init(empty + 8 * i, 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "n"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  // both CTAs' barriers are initialised before either CTA signals its peer
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t issued = 0;
+      for (uint32_t k = 0; k < a.nstages; k++) {
+        const uint32_t s = k % a.stages, use = k / a.stages;
+        if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) break;
+        const uint32_t fb = map_to_rank(full + 8 * s, 0);
+        if (rank == 0) mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
+        const uint32_t dst = smem_u32(smem + s * stage_bytes);
+        tma_load_2d_pair(dst, &tmA, (int)(k * 128), (int)m0, fb);
+        tma_load_2d_pair(dst + kPairHalfBytes, &tmB, (int)(k * 128), (int)(n0 + 128 * rank), fb);
+        issued = k + 1;
+      }
+      // After an abort the leader waits (bounded) for the loads its barriers
+      // expect.  The peer's loads complete on the leader's barriers, which the
+      // peer cannot wait on, so a stopped peer sleeps ~0.2 ms instead: far
+      // longer than a 16 KB load takes to land in its shared memory.
+      if (*abort_flag) {
+        if (rank == 0) {
+          for (uint32_t k = (issued > (uint32_t)a.stages ? issued - a.stages : 0); k < issued; k++)
+            mbar_drain(full + 8 * (k % a.stages), (k / a.stages) & 1);
+        } else {
+          for (int i = 0; i < 200; i++) __nanosleep(1000);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && rank == 0) {
+      bool ok = true;
+      for (uint32_t k = 0; k < a.nstages && ok; k++) {
+        const uint32_t s = k % a.stages;
+        if (!mbar_wait(full + 8 * s, (k / a.stages) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t base = smem_u32(smem + s * stage_bytes);
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++)
+          mma_f8_pair(tmem, sw128_desc(base + kk * 32), sw128_desc(base + kPairHalfBytes + kk * 32), a.idesc,
+                      (k | kk) != 0);
+        mma_commit_pair(empty + 8 * s);
+      }
+      if (ok) {
+        mma_commit_pair(acc_full);
+      } else {  // issued MMAs finish before TMEM is freed
+        asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done)
+                     : "memory");
+        mbar_drain(mma_done, 0);
+      }
+    }
+  } else {
+    if (__all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag))) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int q = warp & 3;
+      const uint64_t gm = m0 + q * 32 + lane;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int col = 0; col < 256; col += 32) {
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+              "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+              "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr + (uint32_t)col));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (gm < a.M) {
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const uint64_t gn = n0 + col + j;
+            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(256));
+  }
+}
+
 // Throughput probe: one CTA per SM, one thread issuing back-to-back
 // tcgen05.mma (M=128, N=256) from fixed zeroed shared tiles; kind 0 = e4m3
 // (K=32), kind 1 = bf16 (K=16).  A commit + bounded wait closes every 64 MMAs.
@@ -666,6 +841,36 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   a.M = c->lhs.nrows;
   a.N = c->rhs.nrows;
   a.nstages = (uint32_t)(c->lhs.ncols_a / 128);
+  if (bn_req == kPairVariant || (bn_req < 0 && a.M >= 256 && a.N >= 256)) {  // 256 x 256 tiles on SM pairs
+    a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+    const size_t stage_bytes = 2 * kPairHalfBytes;
+    // 16 KB of slack past the barriers: no operand read of the last stage can
+    // leave the allocation even if it spanned a whole 256-row tile
+    const size_t slack = kPairHalfBytes;
+    int stages = kPairStagesMax;
+    while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 + slack > kSmemCap) stages--;
+    a.stages = stages;
+    const size_t smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 + slack;
+    cudaError_t e = cudaFuncSetAttribute(gemm_tc_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)(2 * ((a.M + 255) / 256)), (unsigned)((a.N + 255) / 256));
+    cfg.blockDim = dim3(kPairThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel, *reinterpret_cast<const CUtensorMap *>(c->tc_map_da),
+                           *reinterpret_cast<const CUtensorMap *>(c->tc_map_db), a);
+    count_launch();
+    return e != cudaSuccess ? e : cudaGetLastError();
+  }
   const int bn = (bn_req == 128 || bn_req == 256) ? bn_req : (a.N > 128 ? 256 : 128);
   a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
   const size_t stage_bytes = (size_t)(kBM + bn) * kRowB;

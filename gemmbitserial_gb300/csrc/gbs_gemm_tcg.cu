@@ -337,13 +337,15 @@ cudaError_t launch_expand(const ExpandJob &job, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// Digit matrix [nrows_a][ncols_a] of one side, allocated zeroed on first use.
+// Digit matrix [nrows_a][ncols_a] of one side, allocated zeroed on first use
+// (synchronously: kernels on any stream may write it right after).
 cudaError_t ensure_digit_buffer(gbs_ctx *c, int side) {
   if (c->digits[side]) return cudaSuccess;
   const Mat &m = side ? c->rhs : c->lhs;
   const size_t bytes = std::max<size_t>(m.nrows_a * m.ncols_a, 16);
   cudaError_t e = dev_alloc((void **)&c->digits[side], bytes);
   if (e == cudaSuccess) e = cudaMemset(c->digits[side], 0, bytes);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
   c->digit_maps_ready = false;
   c->digits_valid[side] = false;
   return e;

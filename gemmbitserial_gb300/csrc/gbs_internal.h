@@ -134,8 +134,14 @@ struct gbs_ctx {
   uint64_t lhsBlock = 0, rhsBlock = 0;
   int32_t *res = nullptr;     // [N][M]
   int32_t *rowsum = nullptr;  // scratch: row sums, lhs rows at [0, M), rhs rows at [M, M+N)
-  void *stage = nullptr;      // device staging for host-side imports
-  size_t stage_bytes = 0;
+  // host-source imports: per-side device staging, a copy stream and events
+  // that let the packing of each copied chunk overlap the copy of the next
+  void *stage[2] = {nullptr, nullptr};
+  size_t stage_bytes[2] = {0, 0};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_chunk[8] = {};
+  cudaEvent_t ev_packed[2] = {};
+  bool ev_packed_set[2] = {false, false};
   int device = 0;
   int pipe = GBS_PIPE_AUTO;
   int variant = -1;  // pipe variant: CUDA-core tile class (0..2) or tensor-core N tile (128/256); -1 = built-in rule
@@ -165,6 +171,9 @@ cudaError_t dev_alloc(void **p, size_t bytes);
 
 // kernels (gbs_pack.cu)
 cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major, cudaStream_t s);
+// row-major pack of padded rows [r0, r1); with digits set also the e4m3 digit rows (table dtab[4])
+cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t r0, uint64_t r1, uint8_t *digits,
+                             const uint32_t *dtab, cudaStream_t s);
 cudaError_t launch_rowsum(const Mat &m, int32_t *dst, cudaStream_t s);
 cudaError_t launch_export(const Mat &m, int32_t *dst, cudaStream_t s);
 
@@ -184,6 +193,7 @@ bool bmma_supported(int wa, int wb, int use_xor);
 bool tc_supported(const gbs_ctx *c);
 cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
+constexpr int kPairVariant = 512;  // tensor-core variant: 256 x 256 tiles on SM pairs (tcgen05 cta_group::2)
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 

@@ -87,15 +87,51 @@ __device__ __forceinline__ void pack_segment(const void *__restrict__ src, int d
   emit_planes(nbits, nrows_a, wpr, planes, r, seg, lane, q);
 }
 
+// e4m3 digits of 4 codes (one per byte): the code's low nbits bits index the
+// 16-entry byte table tab (byte-permute lookup; PRMT reads only 3 index bits,
+// so 4-bit codes take the high half of the table when bit 3 is set).
+__device__ __forceinline__ uint32_t digits4(uint32_t x, int nbits, uint4 tab) {
+  const uint32_t xm = x & (0x01010101u * ((1u << nbits) - 1u));
+  const uint32_t t = xm | (xm >> 4);                  // byte 0 = c0 | c1 << 4, byte 2 = c2 | c3 << 4
+  const uint32_t sel = __byte_perm(t, 0u, 0x0020u);   // nibbles c0 c1 c2 c3
+  if (nbits <= 3) return __byte_perm(tab.x, tab.y, sel);
+  const uint32_t lo = __byte_perm(tab.x, tab.y, sel & 0x7777u);
+  const uint32_t hi = __byte_perm(tab.z, tab.w, sel & 0x7777u);
+  const uint32_t m = ((xm >> 3) & 0x01010101u) * 0xFFu;
+  return (lo & ~m) | (hi & m);
+}
+
+// Row-major pack of padded rows [row0, row0 + nrows_launch).  With digits
+// set, each lane also writes the e4m3 digits of its 16 columns into the
+// digit matrix [nrows_a][64 * wpr] (0 past nrows and past ncols), the
+// operand of the tensor-core pipe.
 __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
                                                      int nbits, uint64_t nrows, uint64_t ncols,
                                                      uint64_t nrows_a, uint64_t wpr, int vec,
-                                                     uint64_t *__restrict__ planes) {
+                                                     uint64_t *__restrict__ planes, uint64_t row0,
+                                                     uint64_t nrows_launch, uint8_t *__restrict__ digits,
+                                                     uint4 dtab) {
   const uint64_t segs = (wpr + 7) / 8;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (warp >= nrows_a * segs) return;  // warp-uniform
-  pack_segment(src, dtype, bipolar, nbits, nrows, ncols, nrows_a, wpr, vec, planes, warp / segs, warp % segs,
-               threadIdx.x & 31);
+  if (warp >= nrows_launch * segs) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  const uint64_t r = row0 + warp / segs, seg = warp % segs;
+  uint32_t q[4];
+  load_codes(src, dtype, bipolar, nrows, ncols, vec, r, seg, lane, q);
+  emit_planes(nbits, nrows_a, wpr, planes, r, seg, lane, q);
+  const uint64_t col0 = seg * 512 + (uint64_t)lane * 16;
+  if (digits && col0 < wpr * 64) {
+    uint32_t d[4] = {0u, 0u, 0u, 0u};
+    if (r < nrows) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        d[i] = digits4(q[i], nbits, dtab);
+        const uint64_t c = col0 + 4 * i;
+        if (c + 4 > ncols) d[i] &= c >= ncols ? 0u : (0xFFFFFFFFu >> (8 * (4 - (ncols - c))));
+      }
+    }
+    *reinterpret_cast<uint4 *>(digits + r * wpr * 64 + col0) = make_uint4(d[0], d[1], d[2], d[3]);
+  }
 }
 
 // Index of the job owning global warp w: the last job with warp0 <= w.
@@ -258,15 +294,26 @@ inline unsigned blocks_for(uint64_t threads, unsigned per_block) {
 
 }  // namespace
 
+cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t r0, uint64_t r1, uint8_t *digits,
+                             const uint32_t *dtab, cudaStream_t s) {
+  if (m.nrows_a == 0 || m.wpr() == 0 || r1 <= r0) return cudaSuccess;
+  const int bip = m.bipolar() ? 1 : 0;
+  const size_t esz = dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1;
+  const int vec = (esz == 1 && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0) ? 1 : 0;
+  const uint64_t warps = (r1 - r0) * ((m.wpr() + 7) / 8);
+  const uint4 tab = dtab ? make_uint4(dtab[0], dtab[1], dtab[2], dtab[3]) : make_uint4(0u, 0u, 0u, 0u);
+  pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
+                                                          m.nrows_a, m.wpr(), vec, m.planes, r0, r1 - r0,
+                                                          digits, tab);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major, cudaStream_t s) {
   if (m.nrows_a == 0 || m.wpr() == 0) return cudaSuccess;
   const int bip = m.bipolar() ? 1 : 0;
   if (!col_major) {
-    const size_t esz = dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1;
-    const int vec = (esz == 1 && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0) ? 1 : 0;
-    const uint64_t warps = m.nrows_a * ((m.wpr() + 7) / 8);
-    pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
-                                                            m.nrows_a, m.wpr(), vec, m.planes);
+    return launch_pack_rows(m, src, dtype, 0, m.nrows_a, nullptr, nullptr, s);
   } else {
     const uint64_t warps = (m.nrows_a / 32) * m.wpr();
     pack_colmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,

@@ -295,6 +295,7 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
   if (tc_supported(c)) {
     cands[nc++] = Cand{GBS_PIPE_TC, 128};
     cands[nc++] = Cand{GBS_PIPE_TC, 256};
+    cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant};
     cands[nc++] = Cand{GBS_PIPE_TC_SMEM, 256};
     cands[nc++] = Cand{GBS_PIPE_TC_PAIRS, 128};
   }

@@ -140,7 +140,9 @@ GBS_API int gbs_export(gbs_ctx *ctx, int side, int32_t *dst, void *stream);
 GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
 
 /* Forces the variant of a context's pipe: CUDA-core tile class (0: 64x64,
- * 1: 32x128, 2: 16x256 outputs per CTA) or tensor-core N tile (128 or 256);
+ * 1: 32x128, 2: 16x256 outputs per CTA), tensor-core N tile (128 or 256 rows
+ * of rhs per 128-row lhs tile on one SM), or 512 for GBS_PIPE_TC: 256 x 256
+ * tiles computed by pairs of SMs (tcgen05 cta_group::2, two-CTA clusters);
  * -1 restores the built-in rule.  No reference counterpart. */
 GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
 

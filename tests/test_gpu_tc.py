@@ -25,11 +25,17 @@ def lib(gbs_lib):
     return gbs_lib
 
 
+PAIR = (_capi.GBS_PIPE_TC, 512)  # 256 x 256 tiles on SM pairs
+
+
 def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True, pipe=_capi.GBS_PIPE_TC):
     M, K = A.shape
     N = B.shape[0]
     ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
     try:
+        if isinstance(pipe, tuple):
+            pipe, variant = pipe
+            _capi.check(_capi.load().gbs_set_variant(ctx._h, variant))
         ctx.set_pipe(pipe)
         if expect_tc:
             assert ctx.pipe == pipe, "tensor-core pipe not applicable"
@@ -56,8 +62,8 @@ def test_tc_small_first():
 ENCS = [(1, "u"), (1, "b"), (2, "u"), (2, "s"), (3, "u"), (3, "s"), (4, "u"), (4, "s")]
 
 
-MODES = [_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS]
-MODE_IDS = ["hbm-digits", "smem-digits", "pairs"]
+MODES = [_capi.GBS_PIPE_TC, PAIR, _capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS]
+MODE_IDS = ["hbm-digits", "hbm-digits-sm-pair", "smem-digits", "plane-pairs"]
 
 
 @pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
