@@ -87,6 +87,10 @@ void free_ctx_buffers(gbs_ctx *c) {
   for (cudaEvent_t ev : c->ev_chunk)
     if (ev) cudaEventDestroy(ev);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->plan1) {
+    tcg_plan_free(c->plan1);
+    delete c->plan1;
+  }
   if (c->digits[0]) cudaFree(c->digits[0]);
   if (c->digits[1]) cudaFree(c->digits[1]);
 }
@@ -129,7 +133,7 @@ int choose_pipe(const gbs_ctx *c);
 // the CUDA cores for shapes it does not cover.
 int effective_pipe(const gbs_ctx *c) {
   const int p = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
-  if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && !tc_supported(c)) return GBS_PIPE_POPC;
+  if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && !tc_exact(c, p)) return GBS_PIPE_POPC;
   return p;
 }
 

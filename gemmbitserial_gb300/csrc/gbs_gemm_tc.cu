@@ -739,15 +739,17 @@ uint64_t tc_max_abs(const Mat &m) { return max_abs(m); }
 
 bool tc_encoder_available() { return encode_fn() != nullptr; }
 
-// The tensor-core pipe applies when every partial sum stays exact in fp32,
-// at most 4 planes per operand and 5 in total fit the operand ring, and
-// both dimensions fill at least half a tile.
-bool tc_supported(const gbs_ctx *c) {
+// A tensor-core pipe is exact for a context when every partial sum stays an
+// integer below 2^24 in fp32 and each operand's values fit e4m3 exactly (at
+// most 4 bits).  The shared-memory variants also need every plane of a stage
+// in their operand ring: at most 5 planes in total.
+bool tc_exact(const gbs_ctx *c, int pipe) {
   const Mat &A = c->lhs, &B = c->rhs;
-  if (A.nbits > 4 || B.nbits > 4 || A.nbits + B.nbits > 5) return false;
-  if (A.nrows < 64 || B.nrows < 64 || A.ncols == 0) return false;
+  if (A.nbits > 4 || B.nbits > 4 || A.nrows == 0 || B.nrows == 0 || A.ncols == 0) return false;
+  if ((pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM) && A.nbits + B.nbits > 5) return false;
   if ((double)A.ncols * (double)max_abs(A) * (double)max_abs(B) >= 16777216.0) return false;
-  if (A.nrows_a * A.nbits > (1ull << 31) || B.nrows_a * B.nbits > (1ull << 31)) return false;
+  if (A.nrows_a * A.nbits > (1ull << 31) || B.nrows_a * B.nbits > (1ull << 31) || A.ncols_a >= (1ull << 31))
+    return false;
   return encode_fn() != nullptr;
 }
 
@@ -841,7 +843,20 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   a.M = c->lhs.nrows;
   a.N = c->rhs.nrows;
   a.nstages = (uint32_t)(c->lhs.ncols_a / 128);
-  if (bn_req == kPairVariant || (bn_req < 0 && a.M >= 256 && a.N >= 256)) {  // 256 x 256 tiles on SM pairs
+  if (bn_req < 0 && (a.M < 256 || a.N < 256)) {
+    // a side of fewer than 256 rows: the persistent kernel over a one-problem
+    // plan (larger side as the MMA's 128-row operand, MMA N down to 16)
+    if (!c->plan1_ready) {
+      if (!c->plan1) c->plan1 = new TcgPlan();
+      gbs_ctx *one[1] = {c};
+      if (tcg_plan_build(c->plan1, one, 1) != GBS_OK) return cudaErrorInvalidValue;
+      c->plan1_ready = true;
+    }
+    uint32_t *err = tc_error_ptr();
+    if (!err) return cudaErrorInvalidSymbol;
+    return tcg_gemm(*c->plan1, err, s);
+  }
+  if (bn_req == kPairVariant || bn_req < 0) {  // 256 x 256 tiles on SM pairs
     a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
     const size_t stage_bytes = 2 * kPairHalfBytes;
     // 16 KB of slack past the barriers: no operand read of the last stage can
@@ -933,6 +948,21 @@ int tc_peaks(double *f8, double *bf16) {
   if (f8) *f8 = out[0];
   if (bf16) *bf16 = out[1];
   return GBS_OK;
+}
+
+uint32_t *tc_error_ptr() {
+  static uint32_t *addr[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_tc_error) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    addr[dev] = static_cast<uint32_t *>(p);
+  }
+  return addr[dev];
 }
 
 uint32_t tc_error_word() {

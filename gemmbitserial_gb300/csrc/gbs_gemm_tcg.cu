@@ -347,19 +347,14 @@ cudaError_t ensure_digit_buffer(gbs_ctx *c, int side) {
   if (e == cudaSuccess) e = cudaMemset(c->digits[side], 0, bytes);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   c->digit_maps_ready = false;
+  c->plan1_ready = false;
   c->digits_valid[side] = false;
   return e;
 }
 
 // The digit kernel is exact when every partial sum stays below 2^24 in fp32
 // and each operand's values fit e4m3 exactly (at most 4 bits).
-bool tcg_eligible(const gbs_ctx *c) {
-  const Mat &A = c->lhs, &B = c->rhs;
-  if (A.nbits > 4 || B.nbits > 4 || A.nrows == 0 || B.nrows == 0 || A.ncols == 0) return false;
-  if ((double)A.ncols * (double)tc_max_abs(A) * (double)tc_max_abs(B) >= 16777216.0) return false;
-  if (A.nrows_a >= (1ull << 31) || B.nrows_a >= (1ull << 31) || A.ncols_a >= (1ull << 31)) return false;
-  return tc_encoder_available();
-}
+bool tcg_eligible(const gbs_ctx *c) { return tc_exact(c, GBS_PIPE_TC); }
 
 // Digits cost about one HBM byte per element of the larger operand; the
 // CUDA-core popcount kernel costs 2 * min(M, N) * wA * wB bit operations per

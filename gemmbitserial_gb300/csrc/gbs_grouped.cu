@@ -41,6 +41,7 @@ struct gbs_group {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   gbs::TcgPlan tc;  // problems on the tensor-core kernel
+  std::vector<char> is_tc;  // per problem: on the tensor-core kernel
   uint64_t launches_per_replay = 0;
   uint32_t popc_tiles = 0;
 };
@@ -105,8 +106,13 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
       j.issigned = m.issigned;
       j.dtype = dt;
       j.vec = (dt == GBS_I8 || dt == GBS_U8) && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0;
+      j.segs = (uint32_t)pack_segs_per_row(m.wpr());
+      if (g->is_tc[p]) {  // tensor-core problem: the import writes its digit matrices too
+        j.digits = g->ctxs[p]->digits[side];
+        tc_digit_table(m, j.dtab);
+      }
       j.warp0 = warps;
-      warps += m.nrows_a * ((m.wpr() + 7) / 8);
+      warps += m.nrows_a * j.segs;
       jobs.push_back(j);
     }
   }
@@ -185,7 +191,8 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
       return fail(GBS_EINVAL, "gbs_group_create: contexts must live on the current device");
     }
     g->ctxs.push_back(c);
-    if (mode != 1 && tcg_eligible(c) && (mode == 2 || tcg_preferred(c))) {
+    g->is_tc.push_back(mode != 1 && tcg_eligible(c) && (mode == 2 || tcg_preferred(c)) ? 1 : 0);
+    if (g->is_tc.back()) {
       tc_ctxs.push_back(c);
       GroupProblem none;  // keeps the popcount table indexed by problem
       memset(&none, 0, sizeof(none));
@@ -294,8 +301,7 @@ int gbs_group_import(gbs_group *g, const void *const *lhs_srcs, const void *cons
   cudaError_t e = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_import: pack kernel");
   for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
-  e = tcg_expand(g->tc, (cudaStream_t)stream);
-  if (e != cudaSuccess) return cuda_fail(e, "gbs_group_import: digit expansion");
+  for (gbs_ctx *c : g->tc.ctxs) c->digits_valid[0] = c->digits_valid[1] = true;  // written by the pack
   return GBS_OK;
 }
 
@@ -334,17 +340,18 @@ int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *con
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: begin capture");
   cudaError_t ke = cudaSuccess;
   if (with_pack) ke = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, s);
-  if (ke == cudaSuccess && with_pack) ke = tcg_expand(g->tc, s);
   if (ke == cudaSuccess) ke = enqueue_gemm(g, s);
   e = cudaStreamEndCapture(s, &g->graph);
   if (ke != cudaSuccess) return cuda_fail(ke, "gbs_group_capture: enqueue");
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: end capture");
   e = cudaGraphInstantiate(&g->exec, g->graph, 0);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_capture: instantiate");
-  g->launches_per_replay = (with_pack && g->npack ? 1 : 0) + (with_pack && g->tc.njobs ? 1 : 0) +
-                           (g->popc_tiles ? 1 + (g->nrs ? 1 : 0) : 0) + (g->tc.ntiles ? 1 : 0);
-  if (with_pack)
+  g->launches_per_replay = (with_pack && g->npack ? 1 : 0) + (g->popc_tiles ? 1 + (g->nrs ? 1 : 0) : 0) +
+                           (g->tc.ntiles ? 1 : 0);
+  if (with_pack) {
     for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
+    for (gbs_ctx *c : g->tc.ctxs) c->digits_valid[0] = c->digits_valid[1] = true;  // each replay packs them
+  }
   return GBS_OK;
 }
 

@@ -67,12 +67,17 @@ struct GroupTile {
 };
 
 // One operand of a grouped import / row-sum pass; warp0 = first global warp.
+// With digits set, the import also writes the operand's e4m3 digit matrix
+// [nrows_a][64 * wpr] (table dtab), the operand of the tensor-core pipe.
 struct PackJob {
   const void *src;
   uint64_t *planes;
   int32_t *rowsum;
+  uint8_t *digits;
   uint64_t nrows, ncols, nrows_a, wpr, warp0;
   int nbits, issigned, dtype, vec;
+  uint32_t segs;  // 512-column segments per row
+  uint32_t dtab[4];
 };
 
 // One problem of the persistent tensor-core kernel (device resident).  The
@@ -156,6 +161,9 @@ struct gbs_ctx {
   alignas(64) unsigned char tc_map_da[128];
   alignas(64) unsigned char tc_map_db[128];
   bool digit_maps_ready = false;
+  // one-problem plan of the persistent tensor-core kernel (shapes with a side under 256 rows)
+  gbs::TcgPlan *plan1 = nullptr;
+  bool plan1_ready = false;
 };
 
 namespace gbs {
@@ -171,6 +179,8 @@ cudaError_t dev_alloc(void **p, size_t bytes);
 
 // kernels (gbs_pack.cu)
 cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major, cudaStream_t s);
+// units of the row-major pack kernels: 1024-column segments per row
+inline uint64_t pack_segs_per_row(uint64_t wpr) { return (wpr * 64 + 1023) / 1024; }
 // row-major pack of padded rows [r0, r1); with digits set also the e4m3 digit rows (table dtab[4])
 cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t r0, uint64_t r1, uint8_t *digits,
                              const uint32_t *dtab, cudaStream_t s);
@@ -190,7 +200,8 @@ cudaError_t launch_pack_grouped(const PackJob *jobs, int njobs, uint64_t total_w
 cudaError_t launch_rowsum_grouped(const PackJob *jobs, int njobs, uint64_t total_warps, cudaStream_t s);
 cudaError_t launch_gemm_bmma(const GemmShape &g, const Epilogue &e, cudaStream_t s);
 bool bmma_supported(int wa, int wb, int use_xor);
-bool tc_supported(const gbs_ctx *c);
+bool tc_exact(const gbs_ctx *c, int pipe);
+uint32_t *tc_error_ptr();
 cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
 constexpr int kPairVariant = 512;  // tensor-core variant: 256 x 256 tiles on SM pairs (tcgen05 cta_group::2)

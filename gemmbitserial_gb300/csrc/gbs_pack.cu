@@ -38,53 +38,50 @@ __device__ __forceinline__ uint32_t nibble(uint32_t x, int b) {
   return ((((x >> b) & 0x01010101u) * 0x00204081u) >> 21) & 0xfu;
 }
 
-// Row-major pack of one 512-column segment (8 words) of padded row r by one
-// warp; lane l owns columns [16l, 16l+16) of the segment, i.e. a quarter of
-// word l/4.  Rows >= nrows and columns >= ncols produce zero bits.
-// load_codes fetches the lane's 16 codes; emit_planes gathers and stores them.
-__device__ __forceinline__ void load_codes(const void *__restrict__ src, int dtype, int bipolar, uint64_t nrows,
-                                           uint64_t ncols, int vec, uint64_t r, uint64_t seg, int lane,
-                                           uint32_t (&q)[4]) {
-  const uint64_t col0 = seg * 512 + (uint64_t)lane * 16;
-  q[0] = q[1] = q[2] = q[3] = 0u;  // 16 codes, 4 per word, byte j%4 of q[j/4]
-  if (r < nrows && col0 < ncols) {
-    const uint64_t base = r * ncols + col0;
-    if (vec) {  // 1-byte elements, 16-byte aligned rows
-      uint4 v = *reinterpret_cast<const uint4 *>((const uint8_t *)src + base);
-      q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w;
-      if (bipolar && dtype == GBS_I8) {
+// Row-major packing: a warp takes a 1024-column segment of one padded row;
+// lane l owns the 32 columns [seg*1024 + 32l, +32).  Its 32 codes (byte j%4
+// of q[j/4]) give, per plane, one whole 32-bit half of a plane word, so the
+// 32 lanes store 128 contiguous bytes per plane with no shuffles.
+constexpr int kSegCols = 1024;
+
+__host__ __device__ inline uint64_t segs_per_row(uint64_t wpr) { return (wpr * 64 + kSegCols - 1) / kSegCols; }
+
+__device__ __forceinline__ void load_codes32(const void *__restrict__ src, int dtype, int bipolar, uint64_t nrows,
+                                             uint64_t ncols, int vec, uint64_t r, uint64_t col0,
+                                             uint32_t (&q)[8]) {
 #pragma unroll
-        for (int i = 0; i < 4; i++) q[i] = __vcmpgts4(q[i], 0u) & 0x01010101u;
-      }
-    } else {
-#pragma unroll 4
-      for (int j = 0; j < 16; j++) {
-        if (col0 + j < ncols) q[j >> 2] |= code_of(load_elem(src, dtype, base + j), dtype, bipolar) << (8 * (j & 3));
-      }
+  for (int i = 0; i < 8; i++) q[i] = 0u;
+  if (r >= nrows || col0 >= ncols) return;
+  const uint64_t base = r * ncols + col0;
+  if (vec) {  // 1-byte elements, 16-byte aligned rows, ncols % 16 == 0
+    const uint4 *p = reinterpret_cast<const uint4 *>((const uint8_t *)src + base);
+    const uint4 v0 = p[0];
+    q[0] = v0.x; q[1] = v0.y; q[2] = v0.z; q[3] = v0.w;
+    if (col0 + 32 <= ncols) {
+      const uint4 v1 = p[1];
+      q[4] = v1.x; q[5] = v1.y; q[6] = v1.z; q[7] = v1.w;
     }
+    if (bipolar && dtype == GBS_I8) {
+#pragma unroll
+      for (int i = 0; i < 8; i++) q[i] = __vcmpgts4(q[i], 0u) & 0x01010101u;
+    }
+  } else {
+#pragma unroll 4
+    for (int j = 0; j < 32; j++)
+      if (col0 + j < ncols) q[j >> 2] |= code_of(load_elem(src, dtype, base + j), dtype, bipolar) << (8 * (j & 3));
   }
 }
 
-__device__ __forceinline__ void emit_planes(int nbits, uint64_t nrows_a, uint64_t wpr, uint64_t *__restrict__ planes,
-                                            uint64_t r, uint64_t seg, int lane, const uint32_t (&q)[4]) {
-  const uint64_t w = seg * 8 + (lane >> 2);
-  const uint64_t plane_words = nrows_a * wpr;
+__device__ __forceinline__ void emit_planes32(int nbits, uint64_t nrows_a, uint64_t wpr, uint64_t *__restrict__ planes,
+                                              uint64_t r, uint64_t col0, const uint32_t (&q)[8]) {
+  uint32_t *p32 = reinterpret_cast<uint32_t *>(planes);  // little-endian halves of the u64 plane words
+  const uint64_t row32 = 2 * wpr, idx = r * row32 + (col0 >> 5), plane32 = nrows_a * row32;
   for (int b = 0; b < nbits; b++) {
-    uint32_t m16 = nibble(q[0], b) | (nibble(q[1], b) << 4) | (nibble(q[2], b) << 8) | (nibble(q[3], b) << 12);
-    uint64_t v = (uint64_t)m16 << (16 * (lane & 3));
-    v |= __shfl_xor_sync(kFull, v, 1);
-    v |= __shfl_xor_sync(kFull, v, 2);
-    if ((lane & 3) == 0 && w < wpr) planes[b * plane_words + r * wpr + w] = v;
+    uint32_t w = 0u;
+#pragma unroll
+    for (int i = 0; i < 8; i++) w |= nibble(q[i], b) << (4 * i);
+    p32[b * plane32 + idx] = w;
   }
-}
-
-__device__ __forceinline__ void pack_segment(const void *__restrict__ src, int dtype, int bipolar, int nbits,
-                                             uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr,
-                                             int vec, uint64_t *__restrict__ planes, uint64_t r, uint64_t seg,
-                                             int lane) {
-  uint32_t q[4];
-  load_codes(src, dtype, bipolar, nrows, ncols, vec, r, seg, lane, q);
-  emit_planes(nbits, nrows_a, wpr, planes, r, seg, lane, q);
 }
 
 // e4m3 digits of 4 codes (one per byte): the code's low nbits bits index the
@@ -101,37 +98,53 @@ __device__ __forceinline__ uint32_t digits4(uint32_t x, int nbits, uint4 tab) {
   return (lo & ~m) | (hi & m);
 }
 
+// The lane's 32 digits of padded row r (0 past nrows and past ncols) into the
+// digit matrix [nrows_a][64 * wpr].
+__device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int nbits, uint64_t nrows,
+                                               uint64_t ncols, uint64_t wpr, uint4 tab, uint64_t r, uint64_t col0,
+                                               const uint32_t (&q)[8]) {
+  uint32_t d[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    d[i] = 0u;
+    if (r < nrows) {
+      d[i] = digits4(q[i], nbits, tab);
+      const uint64_t c = col0 + 4 * i;
+      if (c + 4 > ncols) d[i] &= c >= ncols ? 0u : (0xFFFFFFFFu >> (8 * (4 - (ncols - c))));
+    }
+  }
+  uint4 *dst = reinterpret_cast<uint4 *>(digits + r * wpr * 64 + col0);
+  dst[0] = make_uint4(d[0], d[1], d[2], d[3]);
+  dst[1] = make_uint4(d[4], d[5], d[6], d[7]);
+}
+
+// One 1024-column unit: codes, planes and (optionally) digits of the lane's 32 columns.
+__device__ __forceinline__ void pack_unit(const void *__restrict__ src, int dtype, int bipolar, int nbits,
+                                          uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr, int vec,
+                                          uint64_t *__restrict__ planes, uint8_t *__restrict__ digits, uint4 dtab,
+                                          uint64_t r, uint64_t seg, int lane) {
+  const uint64_t col0 = seg * kSegCols + (uint64_t)lane * 32;
+  if (col0 >= wpr * 64) return;  // past the padded row
+  uint32_t q[8];
+  load_codes32(src, dtype, bipolar, nrows, ncols, vec, r, col0, q);
+  emit_planes32(nbits, nrows_a, wpr, planes, r, col0, q);
+  if (digits) write_digits32(digits, nbits, nrows, ncols, wpr, dtab, r, col0, q);
+}
+
 // Row-major pack of padded rows [row0, row0 + nrows_launch).  With digits
-// set, each lane also writes the e4m3 digits of its 16 columns into the
-// digit matrix [nrows_a][64 * wpr] (0 past nrows and past ncols), the
-// operand of the tensor-core pipe.
+// set, the lanes also write the rows' e4m3 digits (the tensor-core pipe's
+// operand), from the same loads.
 __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
                                                      int nbits, uint64_t nrows, uint64_t ncols,
                                                      uint64_t nrows_a, uint64_t wpr, int vec,
                                                      uint64_t *__restrict__ planes, uint64_t row0,
                                                      uint64_t nrows_launch, uint8_t *__restrict__ digits,
                                                      uint4 dtab) {
-  const uint64_t segs = (wpr + 7) / 8;
+  const uint64_t segs = segs_per_row(wpr);
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= nrows_launch * segs) return;  // warp-uniform
-  const int lane = threadIdx.x & 31;
-  const uint64_t r = row0 + warp / segs, seg = warp % segs;
-  uint32_t q[4];
-  load_codes(src, dtype, bipolar, nrows, ncols, vec, r, seg, lane, q);
-  emit_planes(nbits, nrows_a, wpr, planes, r, seg, lane, q);
-  const uint64_t col0 = seg * 512 + (uint64_t)lane * 16;
-  if (digits && col0 < wpr * 64) {
-    uint32_t d[4] = {0u, 0u, 0u, 0u};
-    if (r < nrows) {
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        d[i] = digits4(q[i], nbits, dtab);
-        const uint64_t c = col0 + 4 * i;
-        if (c + 4 > ncols) d[i] &= c >= ncols ? 0u : (0xFFFFFFFFu >> (8 * (4 - (ncols - c))));
-      }
-    }
-    *reinterpret_cast<uint4 *>(digits + r * wpr * 64 + col0) = make_uint4(d[0], d[1], d[2], d[3]);
-  }
+  pack_unit(src, dtype, bipolar, nbits, nrows, ncols, nrows_a, wpr, vec, planes, digits, dtab, row0 + warp / segs,
+            warp % segs, threadIdx.x & 31);
 }
 
 // Index of the job owning global warp w: the last job with warp0 <= w.
@@ -146,10 +159,10 @@ __device__ __forceinline__ int find_job(const PackJob *jobs, int njobs, uint64_t
 }
 
 // Grouped import: one launch packs every operand of a grouped GEMM
-// (row-major sources); global segment units are numbered across the jobs.
-// A warp takes kRun consecutive units per step: one job lookup, then the
-// loads of kPar units are in flight together before any of them is packed.
-constexpr int kRun = 16, kPar = 4;
+// (row-major sources); units (1024-column segments of a row) are numbered
+// across the jobs.  A warp takes kRun consecutive units: one job lookup,
+// then the units in order.
+constexpr int kRun = 8;
 
 __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ jobs, int njobs, uint64_t total) {
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -157,30 +170,25 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
   for (uint64_t base = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRun; base < total;
        base += nw * kRun) {
     int j = find_job(jobs, njobs, base);
-    for (int u0 = 0; u0 < kRun; u0 += kPar) {
-      uint32_t q[kPar][4];
-      int jj[kPar];
-      uint64_t rr[kPar], ss[kPar];
-#pragma unroll
-      for (int u = 0; u < kPar; u++) {
-        const uint64_t w = base + u0 + u;
-        jj[u] = -1;
-        q[u][0] = q[u][1] = q[u][2] = q[u][3] = 0u;
-        if (w >= total) continue;
-        while (j + 1 < njobs && jobs[j + 1].warp0 <= w) j++;
-        const PackJob &J = jobs[j];
-        const uint64_t local = w - J.warp0, segs = (J.wpr + 7) / 8;
-        jj[u] = j;
-        rr[u] = local / segs;
-        ss[u] = local % segs;
-        load_codes(J.src, J.dtype, J.nbits == 1 && J.issigned, J.nrows, J.ncols, J.vec, rr[u], ss[u], lane, q[u]);
+#pragma unroll 1
+    for (int u = 0; u < kRun; u++) {
+      const uint64_t w = base + u;
+      if (w >= total) break;
+      while (j + 1 < njobs && jobs[j + 1].warp0 <= w) j++;
+      const PackJob &J = jobs[j];
+      const uint64_t local = w - J.warp0;
+      uint64_t r, sg;
+      if (local < 0xFFFFFFFFull) {  // 32-bit division in the common case
+        const uint32_t l32 = (uint32_t)local, r32 = l32 / J.segs;
+        r = r32;
+        sg = l32 - r32 * J.segs;
+      } else {
+        r = local / J.segs;
+        sg = local % J.segs;
       }
-#pragma unroll
-      for (int u = 0; u < kPar; u++) {
-        if (jj[u] < 0) continue;
-        const PackJob &J = jobs[jj[u]];
-        emit_planes(J.nbits, J.nrows_a, J.wpr, J.planes, rr[u], ss[u], lane, q[u]);
-      }
+      const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
+      pack_unit(J.src, J.dtype, J.nbits == 1 && J.issigned, J.nbits, J.nrows, J.ncols, J.nrows_a, J.wpr, J.vec,
+                J.planes, J.digits, tab, r, sg, lane);
     }
   }
 }
@@ -300,7 +308,7 @@ cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t 
   const int bip = m.bipolar() ? 1 : 0;
   const size_t esz = dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1;
   const int vec = (esz == 1 && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0) ? 1 : 0;
-  const uint64_t warps = (r1 - r0) * ((m.wpr() + 7) / 8);
+  const uint64_t warps = (r1 - r0) * segs_per_row(m.wpr());
   const uint4 tab = dtab ? make_uint4(dtab[0], dtab[1], dtab[2], dtab[3]) : make_uint4(0u, 0u, 0u, 0u);
   pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
                                                           m.nrows_a, m.wpr(), vec, m.planes, r0, r1 - r0,

@@ -146,10 +146,10 @@ int choose_pipe(const gbs_ctx *c) {
     if (it != g_store.end()) {
       const int p = it->second.pipe;
       if (p == GBS_PIPE_POPC || p == GBS_PIPE_BMMA) return p;
-      if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && tc_supported(c)) return p;
+      if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && tc_exact(c, p)) return p;
     }
   }
-  return tc_supported(c) ? GBS_PIPE_TC : GBS_PIPE_POPC;
+  return (tc_exact(c, GBS_PIPE_TC) && tcg_preferred(c)) ? GBS_PIPE_TC : GBS_PIPE_POPC;
 }
 
 int tuned_variant(const gbs_ctx *c, int pipe) {
@@ -292,10 +292,13 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
   int nc = 0;
   for (int v = -1; v <= 2; v++) cands[nc++] = Cand{GBS_PIPE_POPC, v};  // -1: built-in tile rule
   cands[nc++] = Cand{GBS_PIPE_BMMA, -1};
-  if (tc_supported(c)) {
+  if (tc_exact(c, GBS_PIPE_TC)) {
+    cands[nc++] = Cand{GBS_PIPE_TC, -1};  // built-in rule: SM pairs, or the persistent kernel for a side < 256
     cands[nc++] = Cand{GBS_PIPE_TC, 128};
     cands[nc++] = Cand{GBS_PIPE_TC, 256};
     cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant};
+  }
+  if (tc_exact(c, GBS_PIPE_TC_SMEM)) {
     cands[nc++] = Cand{GBS_PIPE_TC_SMEM, 256};
     cands[nc++] = Cand{GBS_PIPE_TC_PAIRS, 128};
   }

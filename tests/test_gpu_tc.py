@@ -109,12 +109,36 @@ def test_tc_sums_near_the_exactness_bound():
 
 
 def test_tc_pipe_declines_what_it_cannot_do_exactly():
-    """8-bit operands or K beyond the fp32 bound fall back to the CUDA-core pipe."""
-    for (M, K, N, wa, wb) in [(128, 256, 128, 8, 1), (128, 1 << 21, 128, 4, 1), (16, 256, 128, 1, 1)]:
+    """8-bit operands or K beyond the fp32 bound fall back to the CUDA-core pipe; the
+    shared-memory variants also decline more than 5 planes; AUTO keeps tiny problems
+    on the CUDA cores."""
+    for (M, K, N, wa, wb) in [(128, 256, 128, 8, 1), (128, 1 << 21, 128, 4, 1)]:
         ctx = allocGEMMContext(M, K, N, wa, wb, False, False)
         ctx.set_pipe(_capi.GBS_PIPE_TC)
         assert ctx.pipe == _capi.GBS_PIPE_POPC
         deallocGEMMContext(ctx)
+    ctx = allocGEMMContext(128, 256, 128, 4, 4, False, False)
+    ctx.set_pipe(_capi.GBS_PIPE_TC_SMEM)
+    assert ctx.pipe == _capi.GBS_PIPE_POPC
+    ctx.set_pipe(_capi.GBS_PIPE_TC)
+    assert ctx.pipe == _capi.GBS_PIPE_TC
+    deallocGEMMContext(ctx)
+    ctx = allocGEMMContext(4, 256, 2, 1, 1, False, False)
+    assert ctx.pipe == _capi.GBS_PIPE_POPC
+    deallocGEMMContext(ctx)
+
+
+@pytest.mark.parametrize("shape", [(1, 4096, 3000, 4, "u", 4, "s"), (17, 333, 129, 2, "u", 1, "b"),
+                                   (200, 1000, 96, 3, "s", 2, "u"), (255, 640, 255, 4, "u", 4, "u"),
+                                   (64, 100, 4096, 1, "b", 1, "b")])
+def test_tc_persistent_single_problem(shape):
+    """Shapes with a side under 256 rows run the persistent kernel over a one-problem plan."""
+    M, K, N, wa, ea, wb, eb = shape
+    A = datagen.operand(datagen.SEED_BASE + 700 + M, M, K, wa, ea)
+    B = datagen.operand(datagen.SEED_BASE + 701 + N, N, K, wb, eb)
+    got = tc_gemm(A, B, wa, wb, ea != "u", eb != "u")
+    assert np.array_equal(got, O.oracle_gemm(A, B, wa, wb, ea != "u", eb != "u"))
+    assert _capi.load().gbs_debug_tc_error() == 0
 
 
 def test_tc_peaks_probe():
