@@ -15,6 +15,9 @@
 // contiguous in s).  CTA tile 128 (r) x 128 (k), 8 values of s per stage,
 // 256 threads with 8 x 8 outputs each (two 4-wide groups per dimension for
 // conflict-free float4 shared reads), FP32 FMA accumulation in registers.
+#include <cstdlib>
+#include <cstring>
+
 #include "gbs_internal.h"
 
 namespace gbs {
@@ -236,6 +239,8 @@ extern "C" int gbs_adjoint(gbs_ctx *c, const float *dC, float *dA, float *dB, vo
     }
   }
   cudaStream_t s = (cudaStream_t)stream;
+  const char *mode = getenv("GBS_ADJOINT_PIPE");
+  if (!(mode && !strcmp(mode, "simt")) && adjoint_tc_available()) return adjoint_tc(c, dC, dA, dB, s);
   if (dA) {
     cudaError_t e = launch_adjoint(c->rhs, dC, M, N, true, dA, s);
     if (e != cudaSuccess) return cuda_fail(e, "gbs_adjoint: dA kernel");

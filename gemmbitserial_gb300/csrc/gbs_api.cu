@@ -91,6 +91,7 @@ void free_ctx_buffers(gbs_ctx *c) {
     tcg_plan_free(c->plan1);
     delete c->plan1;
   }
+  adj_plan_free(c->adj);
   if (c->digits[0]) cudaFree(c->digits[0]);
   if (c->digits[1]) cudaFree(c->digits[1]);
 }
@@ -291,6 +292,7 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
   if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_import: cudaSetDevice");
   cudaStream_t s = as_stream(stream);
   c->digits_valid[side] = false;
+  c->vt_valid[side] = false;
   uint8_t *digits = nullptr;
   uint32_t dtab[4] = {0, 0, 0, 0};
   if (!col_major && import_writes_digits(c)) {

@@ -300,7 +300,10 @@ int gbs_group_import(gbs_group *g, const void *const *lhs_srcs, const void *cons
   if (rc != GBS_OK) return rc;
   cudaError_t e = launch_pack_grouped(g->d_pack_jobs, g->npack, g->pack_warps, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_import: pack kernel");
-  for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
+  for (gbs_ctx *c : g->ctxs) {
+    c->lhs.imported = c->rhs.imported = true;
+    c->vt_valid[0] = c->vt_valid[1] = false;
+  }
   for (gbs_ctx *c : g->tc.ctxs) c->digits_valid[0] = c->digits_valid[1] = true;  // written by the pack
   return GBS_OK;
 }
@@ -359,6 +362,8 @@ int gbs_group_replay(gbs_group *g, void *stream) {
   if (!g || !g->exec) return fail(GBS_ESTATE, "gbs_group_replay: capture the group first");
   cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_replay");
+  if (g->npack)  // the replay packs new planes: cached adjoint operands are stale
+    for (gbs_ctx *c : g->ctxs) c->vt_valid[0] = c->vt_valid[1] = false;
   count_launch(g->launches_per_replay);
   return GBS_OK;
 }

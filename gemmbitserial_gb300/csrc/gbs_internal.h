@@ -10,6 +10,8 @@
 
 namespace gbs {
 
+struct AdjPlan;  // workspace of the tensor-core adjoint (gbs_adjoint_tc.cu)
+
 constexpr uint64_t kRowAlign = 256;  // device row padding (rows of a plane): a multiple of every tile's row count
 constexpr uint64_t kColAlign = 256;  // device column padding (bits of a row)
 constexpr int kMaxBits = 8;
@@ -164,6 +166,8 @@ struct gbs_ctx {
   // one-problem plan of the persistent tensor-core kernel (shapes with a side under 256 rows)
   gbs::TcgPlan *plan1 = nullptr;
   bool plan1_ready = false;
+  gbs::AdjPlan *adj = nullptr;  // tensor-core adjoint workspace, built on first use
+  bool vt_valid[2] = {false, false};  // its transposed bf16 operand values match the planes
 };
 
 namespace gbs {
@@ -222,6 +226,10 @@ void tcg_plan_free(TcgPlan *plan);
 cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s);
 cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s);
 cudaError_t ensure_digit_buffer(gbs_ctx *c, int side);
+// tensor-core adjoint (gbs_adjoint_tc.cu)
+int adjoint_tc(gbs_ctx *c, const float *dC, float *dA, float *dB, cudaStream_t s);
+bool adjoint_tc_available();
+void adj_plan_free(AdjPlan *p);
 ExpandJob make_expand_job(const Mat &m, uint8_t *digits);
 cudaError_t launch_expand(const ExpandJob &job, cudaStream_t s);
 int effective_pipe(const gbs_ctx *c);

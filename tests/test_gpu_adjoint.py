@@ -25,6 +25,16 @@ def lib(gbs_lib):
     return gbs_lib
 
 
+@pytest.fixture(params=["tc", "simt"])
+def adjoint_pipe(request, monkeypatch):
+    """GBS_ADJOINT_PIPE: the tensor-core adjoint (default) or the CUDA-core FP32 kernel."""
+    if request.param == "tc":
+        monkeypatch.delenv("GBS_ADJOINT_PIPE", raising=False)
+    else:
+        monkeypatch.setenv("GBS_ADJOINT_PIPE", "simt")
+    return request.param
+
+
 def run_adjoint(A, B, wA, eA, wB, eB, dC):
     import torch
     M, K = A.shape
@@ -64,10 +74,10 @@ def check(A, B, wA, eA, wB, eB, dC):
 
 @pytest.mark.parametrize("enc", [(2, "u", 1, "b"), (3, "u", 2, "s"), (1, "b", 1, "b"), (1, "b", 4, "s"),
                                  (4, "s", 3, "u"), (8, "s", 8, "u"), (1, "u", 1, "u")])
-def test_adjoint_matches_fp64(enc):
+def test_adjoint_matches_fp64(enc, adjoint_pipe):
     wA, eA, wB, eB = enc
     rng = np.random.default_rng(wA * 10 + wB)
-    for (M, K, N) in [(96, 320, 80), (130, 1000, 257), (1, 64, 3), (300, 131, 7)]:
+    for (M, K, N) in [(96, 320, 80), (130, 1000, 257), (1, 64, 3), (300, 131, 7), (257, 700, 333)]:
         A = datagen.operand(int(rng.integers(1 << 30)), M, K, wA, eA)
         B = datagen.operand(int(rng.integers(1 << 30)), N, K, wB, eB)
         dC = datagen.normal_f32(int(rng.integers(1 << 30)), (N, M))
@@ -75,18 +85,18 @@ def test_adjoint_matches_fp64(enc):
         assert na < TOL and ea < TOL and nb < TOL and eb < TOL, (enc, (M, K, N), na, ea, nb, eb)
 
 
-def test_adjoint_qat_layer_full_size():
+def test_adjoint_qat_layer_full_size(adjoint_pipe):
     """The quantised-MLP layer: A 4096 x 2048 2-bit unsigned, B 2048 x 2048 bipolar, dC ~ N(0,1)."""
     M, K, N = 4096, 2048, 2048
     A = datagen.operand(datagen.SEED_BASE + 50, M, K, 2, "u")
     B = datagen.operand(datagen.SEED_BASE + 51, N, K, 1, "b")
     dC = datagen.normal_f32(datagen.SEED_BASE + 52, (N, M))
     (na, ea), (nb, eb) = check(A, B, 2, "u", 1, "b", dC)
-    print(f"dA normwise {na:.3e} elementwise {ea:.3e}; dB normwise {nb:.3e} elementwise {eb:.3e}")
+    print(f"{adjoint_pipe}: dA normwise {na:.3e} elementwise {ea:.3e}; dB normwise {nb:.3e} elementwise {eb:.3e}")
     assert max(na, ea, nb, eb) < TOL
 
 
-def test_adjoint_unit_step_finite_differences():
+def test_adjoint_unit_step_finite_differences(adjoint_pipe):
     """L = sum dC * C is bilinear: one unit step of A[m,k] changes L by exactly dA[m,k]
     (a step of 2 for a bipolar entry changes it by 2*dB[n,k])."""
     import torch
@@ -150,3 +160,30 @@ def test_adjoint_rejects_host_pointers(lib):
     rc = lib.gbs_adjoint(ctx._h, C.c_void_p(host.ctypes.data), C.c_void_p(host.ctypes.data), None, None)
     assert rc == _capi.GBS_EINVAL
     deallocGEMMContext(ctx)
+
+
+def test_adjoint_cache_follows_reimport(adjoint_pipe):
+    """The tensor-core adjoint caches its transposed operand values; a new import replaces them."""
+    import torch
+    M, K, N = 200, 384, 130
+    A1 = datagen.operand(datagen.SEED_BASE + 80, M, K, 3, "s")
+    A2 = datagen.operand(datagen.SEED_BASE + 81, M, K, 3, "s")
+    B1 = datagen.operand(datagen.SEED_BASE + 82, N, K, 2, "u")
+    B2 = datagen.operand(datagen.SEED_BASE + 83, N, K, 2, "u")
+    dC = datagen.normal_f32(datagen.SEED_BASE + 84, (N, M))
+    ctx = allocGEMMContext(M, K, N, 3, 2, True, False)
+    try:
+        d = torch.from_numpy(dC).cuda()
+        dA = torch.empty(M, K, device="cuda")
+        dB = torch.empty(N, K, device="cuda")
+        for A, B in [(A1, B1), (A2, B1), (A2, B2)]:
+            ctx.lhs.importRegular(A)
+            ctx.rhs.importRegular(B)
+            _capi.check(_capi.load().gbs_adjoint(ctx._h, C.c_void_p(d.data_ptr()), C.c_void_p(dA.data_ptr()),
+                                                 C.c_void_p(dB.data_ptr()), None))
+            torch.cuda.synchronize()
+            dA64, dB64 = O.adjoint_fp64(dC, O.decode_values(A, 3, True), O.decode_values(B, 2, False))
+            assert np.max(np.abs(dA.cpu().numpy() - dA64)) <= 1e-6 * np.max(np.abs(dA64))
+            assert np.max(np.abs(dB.cpu().numpy() - dB64)) <= 1e-6 * np.max(np.abs(dB64))
+    finally:
+        deallocGEMMContext(ctx)
