@@ -202,13 +202,14 @@ def read_traffic(kernel, workload):
     return float(m.group(1)) if m else None
 
 
-def measure_grouped(lib, dev, stream, reps=5, warmup=2):
-    """512-problem mix: plain per-problem path vs one persistent grouped launch (and its CUDA graph)."""
+def measure_grouped(lib, dev, stream, reps=5, warmup=2, mix=None, desc=None):
+    """512-problem mix (or another mix): plain per-problem path vs one persistent grouped launch
+    (and its CUDA graph)."""
     import torch
     from gemmbitserial_gb300 import _capi, datagen
     from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext
     from gemmbitserial_gb300.grouped import Group
-    mix = datagen.grouped_mix()
+    mix = datagen.grouped_mix() if mix is None else mix
     gen = torch.Generator(device=dev)
     gen.manual_seed(4321)
     ops = [(datagen.torch_operand(gen, M, K, wA, eA, dev), datagen.torch_operand(gen, N, K, wB, eB, dev))
@@ -261,12 +262,13 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2):
             "plain_pack_gemm_ms": round(t_plain_full, 4), "graph_pack_gemm_ms": round(t_graph, 4),
             "speedup_pack_gemm": round(t_plain_full / t_graph, 3),
             "grouped_gops": round(gops_total / (t_group * 1e-3) / 1e9, 1),
+            "plain_gops": round(gops_total / (t_plain * 1e-3) / 1e9, 1),
             "grouped_tbinops": round(binops / (t_group * 1e-3) / 1e12, 2),
             "tiles": stats["tiles"], "grid": stats["grid"], "smem_bytes": stats["smem_bytes"],
             "popc_problems": stats["popc_problems"], "tc_problems": stats["tc_problems"],
             "tc_tiles": stats["tc_tiles"],
             "parity": "grouped == plain (sampled 14 problems)" if ok else "MISMATCH",
-            "mix": "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
+            "mix": desc or "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
 
 
 def measure_adjoint(lib, dev, stream, reps=10, warmup=3):
@@ -494,6 +496,10 @@ def run_ours(args):
     clocks = clk.summary()
 
     grouped = None if args.no_grouped else measure_grouped(lib, dev, stream)
+    caffenet = None
+    if not args.no_grouped:  # the reference's CaffeNet chain (benchmark.cpp:174-237) as a second group
+        caffenet = measure_grouped(lib, dev, stream, reps=20, warmup=3, mix=datagen.caffenet_mix(),
+                                   desc="CaffeNet chain, 8 GEMMs, 2-bit unsigned x 2-bit unsigned")
     adjoint = None if args.no_adjoint else measure_adjoint(lib, dev, stream)
 
     cpu = None
@@ -514,7 +520,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),
                     "ms_per_step": round(e2e_s * 1e3, 4), "parity": "bit-exact" if e2e_ok else "MISMATCH"},
             "roofline": roof,
-            "grouped": grouped, "adjoint": adjoint,
+            "grouped": grouped, "caffenet": caffenet, "adjoint": adjoint,
             "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
             "wall_s_timed_region": round(t_wall, 4)}
     print(json.dumps(line), flush=True)

@@ -11,7 +11,7 @@ import os
 from . import build as _build
 
 GBS_OK, GBS_EINVAL, GBS_ENOMEM, GBS_ECUDA, GBS_ESTATE, GBS_ETIMEOUT, GBS_EUNSUPPORTED = range(7)
-GBS_I8, GBS_U8, GBS_I16, GBS_I32 = range(4)
+GBS_I8, GBS_U8, GBS_I16, GBS_I32, GBS_F32 = range(5)
 GBS_LHS, GBS_RHS = 0, 1
 GBS_PIPE_AUTO, GBS_PIPE_POPC, GBS_PIPE_BMMA, GBS_PIPE_TC, GBS_PIPE_TC_PAIRS, GBS_PIPE_TC_SMEM = 0, 1, 2, 3, 4, 5
 
@@ -35,6 +35,7 @@ SIGNATURES = {
     "gbs_ctx_free": (i32, [vp]),
     "gbs_ctx_get_info": (i32, [vp, C.POINTER(CtxInfo)]),
     "gbs_import": (i32, [vp, i32, vp, i32, i32, vp]),
+    "gbs_import_quantize": (i32, [vp, i32, vp, vp, i32, i32, i32, vp]),
     "gbs_gemm": (i32, [vp, vp]),
     "gbs_get_result": (i32, [vp, vp, vp]),
     "gbs_sum_rows": (i32, [vp, i32, vp, vp]),

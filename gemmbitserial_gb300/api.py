@@ -41,18 +41,22 @@ def _stream_handle(stream):
     return C.c_void_p(stream.cuda_stream)
 
 
-def _src(arr):
+def _src(arr, allow_float: bool = False):
     """(pointer, dtype code, keepalive) for a numpy array or torch tensor."""
     try:
         import torch
         if isinstance(arr, torch.Tensor):
             t = arr.contiguous()
-            dt = {torch.int8: _capi.GBS_I8, torch.uint8: _capi.GBS_U8,
-                  torch.int16: _capi.GBS_I16, torch.int32: _capi.GBS_I32}[t.dtype]
+            dt = {torch.int8: _capi.GBS_I8, torch.uint8: _capi.GBS_U8, torch.int16: _capi.GBS_I16,
+                  torch.int32: _capi.GBS_I32, torch.float32: _capi.GBS_F32}[t.dtype]
+            if dt == _capi.GBS_F32 and not allow_float:
+                raise TypeError("float input is accepted by importRegularAndQuantize only")
             return C.c_void_p(t.data_ptr()), dt, t
     except ImportError:
         pass
     a = np.ascontiguousarray(arr)
+    if a.dtype == np.float32 and allow_float:
+        return C.c_void_p(a.ctypes.data), _capi.GBS_F32, a
     if a.dtype not in _NP2DT:
         raise TypeError(f"unsupported element type {a.dtype}; use int8, uint8, int16 or int32")
     return C.c_void_p(a.ctypes.data), _NP2DT[a.dtype], a
@@ -107,6 +111,23 @@ class BitSerialMatrix:
         _capi.check(_capi.load().gbs_import(self._ctx._h, self._side, ptr, dt, int(bool(readColMajor)),
                                             _stream_handle(stream)))
         del keep
+
+    def importRegularAndQuantize(self, matrix, thresholds, nThres=None, readColMajor: bool = False,
+                                 stream=None) -> None:
+        """importRegularAndQuantize<T> (gemmbitserial.hpp:282-305): thresholds shaped [nThres][nrows],
+        same element type as matrix (int8, uint8, int16, int32 or float32)."""
+        ptr, dt, keep = _src(matrix, allow_float=True)
+        if nThres is None:
+            nThres = int(thresholds.shape[0]) if thresholds is not None and len(thresholds.shape) == 2 else 0
+        if nThres:
+            tptr, tdt, tkeep = _src(thresholds, allow_float=True)
+            if tdt != dt:
+                raise TypeError("thresholds must have the element type of the matrix")
+        else:
+            tptr, tkeep = None, None
+        _capi.check(_capi.load().gbs_import_quantize(self._ctx._h, self._side, ptr, tptr, int(nThres), dt,
+                                                     int(bool(readColMajor)), _stream_handle(stream)))
+        del keep, tkeep
 
     def planes(self, stream=None) -> np.ndarray:
         """Host copy of the packed planes, shape [nbits, nrows_a, ncols_a/64] (uint64)."""

@@ -82,6 +82,7 @@ void free_ctx_buffers(gbs_ctx *c) {
   if (c->rowsum) cudaFree(c->rowsum);
   for (int side = 0; side < 2; side++) {
     if (c->stage[side]) cudaFree(c->stage[side]);
+    if (c->thr_stage[side]) cudaFree(c->thr_stage[side]);
     if (c->ev_packed[side]) cudaEventDestroy(c->ev_packed[side]);
   }
   for (cudaEvent_t ev : c->ev_chunk)
@@ -245,7 +246,7 @@ int gbs_ctx_get_info(const gbs_ctx *c, gbs_ctx_info *info) {
 namespace {
 
 constexpr int kImportChunks = 8;            // at most this many copy/pack chunks per host import
-constexpr size_t kImportChunkBytes = 2 << 20;
+constexpr size_t kImportChunkBytes = 4 << 20;
 
 // Copy stream and events of host-source imports, created on first use.
 cudaError_t ensure_import_streams(gbs_ctx *c) {
@@ -359,6 +360,75 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
     if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack kernel");
   }
   m.imported = true;
+  return GBS_OK;
+}
+
+int gbs_import_quantize(gbs_ctx *c, int side, const void *src, const void *thresholds, int nthres, int dtype,
+                        int col_major, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_import_quantize: ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_import_quantize: side must be 0 or 1");
+  if (dtype < GBS_I8 || dtype > GBS_F32) return fail(GBS_EINVAL, "gbs_import_quantize: unknown dtype");
+  Mat &m = side ? c->rhs : c->lhs;
+  if (m.issigned)
+    return fail(GBS_EINVAL, "gbs_import_quantize: threshold quantization needs an unsigned matrix");
+  if (nthres < 0) return fail(GBS_EINVAL, "gbs_import_quantize: nthres must be >= 0");
+  const uint64_t n = m.nrows * m.ncols;
+  const size_t esz = dtype == GBS_I16 ? 2 : (dtype == GBS_I32 || dtype == GBS_F32) ? 4 : 1;
+  const size_t tbytes = (size_t)nthres * m.nrows * esz;
+  if ((n && !src) || (tbytes && !thresholds)) return fail(GBS_EINVAL, "gbs_import_quantize: NULL pointer");
+  DeviceGuard g(c->device);
+  if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_import_quantize: cudaSetDevice");
+  cudaStream_t s = as_stream(stream);
+  c->digits_valid[side] = false;
+  c->vt_valid[side] = false;
+  uint8_t *digits = nullptr;
+  uint32_t dtab[4] = {0, 0, 0, 0};
+  if (import_writes_digits(c)) {
+    if (ensure_digit_buffer(c, side) == cudaSuccess) {
+      digits = c->digits[side];
+      tc_digit_table(m, dtab);
+    } else {
+      cudaGetLastError();  // the GEMM expands the digits itself
+    }
+  }
+  bool host = false;
+  const void *dsrc = src, *dthr = thresholds;
+  cudaError_t e = cudaSuccess;
+  if (n && !is_device_ptr(src)) {
+    int rc = ensure_stage(c, side, n * esz, s);
+    if (rc != GBS_OK) return rc;
+    if (c->ev_packed_set[side]) e = cudaStreamWaitEvent(s, c->ev_packed[side], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->stage[side], src, n * esz, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: host-to-device copy");
+    dsrc = c->stage[side];
+    host = true;
+  }
+  if (tbytes && !is_device_ptr(thresholds)) {
+    if (c->thr_bytes[side] < tbytes) {
+      e = cudaStreamSynchronize(s);  // the old buffer may still be read
+      if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: stream sync");
+      if (c->thr_stage[side]) cudaFree(c->thr_stage[side]);
+      c->thr_stage[side] = nullptr;
+      c->thr_bytes[side] = 0;
+      if (dev_alloc(&c->thr_stage[side], tbytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GBS_ENOMEM, "gbs_import_quantize: threshold buffer allocation failed");
+      }
+      c->thr_bytes[side] = tbytes;
+    }
+    e = cudaMemcpyAsync(c->thr_stage[side], thresholds, tbytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: threshold copy");
+    dthr = c->thr_stage[side];
+    host = true;
+  }
+  e = launch_pack_quantize(m, dsrc, dthr, nthres, dtype, col_major ? 1 : 0, digits, dtab, s);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: pack kernel");
+  if (digits) c->digits_valid[side] = true;
+  m.imported = true;
+  if (host) {  // host memory may be reused on return
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: stream sync");
+  }
   return GBS_OK;
 }
 

@@ -159,9 +159,36 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_tiled(TileArgs g) {
   popc_tile<BM, BN, KC, XOR>(g, (uint64_t)blockIdx.x * BM, (uint64_t)blockIdx.y * BN, smem);
 }
 
+// One output (m, n) of a grouped problem by one warp, lanes over the K words
+// (the skinny tile class: matrix-vector and other small-output problems).
+__device__ __forceinline__ void grouped_skinny_output(const GroupProblem &P, uint64_t o, int lane) {
+  const uint64_t n = o / P.M, m = o % P.M;
+  uint32_t acc = 0;
+  for (int i = 0; i < P.wa; i++) {
+    const uint64_t *a = P.A + i * P.a_plane + m * P.wpr;
+    for (int j = 0; j < P.wb; j++) {
+      const uint64_t *b = P.B + j * P.b_plane + n * P.wpr;
+      uint32_t cnt = 0;
+      if (P.use_xor) {
+        for (uint64_t w = lane; w < P.wpr; w += 32) cnt += __popcll(a[w] ^ b[w]);
+      } else {
+        for (uint64_t w = lane; w < P.wpr; w += 32) cnt += __popcll(a[w] & b[w]);
+      }
+      acc += cnt * alpha_of(i, j, P.neg_i, P.neg_j, P.shift, P.use_xor);
+    }
+  }
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
+  if (lane == 0) {
+    const uint32_t v = acc + P.c0 - (P.ra ? (uint32_t)P.ra[m] : 0u) - (P.rb ? (uint32_t)P.rb[n] : 0u);
+    P.C[n * P.M + m] = (int32_t)v;
+  }
+}
+
 // Persistent grouped GEMM: each CTA takes the next tile from the queue until
-// the queue is drained.  A descriptor that fails validation sets a bit in
-// *err and is skipped (no device fault, no wait).
+// the queue is drained.  Tile classes 0-2 are BM x BN output tiles; class 3
+// is kSkinnyTile outputs, one per warp.  A descriptor that fails validation
+// sets a bit in *err and is skipped (no device fault, no wait).
 __global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *__restrict__ probs, int nprob,
                                                            const GroupTile *__restrict__ tiles, uint32_t ntiles,
                                                            uint32_t *counter, uint32_t *err) {
@@ -174,11 +201,21 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *_
     __syncthreads();
     if (t >= ntiles) break;
     const GroupTile tl = tiles[t];
-    if (tl.p >= (uint32_t)nprob || tl.cls > 2) {
+    if (tl.p >= (uint32_t)nprob || tl.cls > kSkinnyCls) {
       if (threadIdx.x == 0) atomicOr(err, 1u);
       continue;
     }
     const GroupProblem &P = probs[tl.p];
+    if (tl.cls == kSkinnyCls) {
+      const uint64_t o0 = (uint64_t)tl.mt * kSkinnyTile;
+      if (o0 >= P.M * P.N || P.wa < 1 || P.wa > kMaxBits || P.wb < 1 || P.wb > kMaxBits) {
+        if (threadIdx.x == 0) atomicOr(err, 2u);
+        continue;
+      }
+      const uint64_t o = o0 + (threadIdx.x >> 5);
+      if (o < P.M * P.N) grouped_skinny_output(P, o, threadIdx.x & 31);
+      continue;
+    }
     const int bm = tile_bm((int)tl.cls), bn = tile_bn((int)tl.cls);
     const uint64_t m0 = (uint64_t)tl.mt * bm, n0 = (uint64_t)tl.nt * bn;
     if (m0 >= P.M || n0 >= P.N || P.wa < 1 || P.wa > kMaxBits || P.wb < 1 || P.wb > kMaxBits) {
@@ -265,6 +302,8 @@ size_t popc_stage_smem(int cls, int wa, int wb, int kc) {
 
 // Tile class for a problem: the narrowest lhs tile that covers M without
 // exceeding the shared-memory cap at the grouped chunk size.
+bool popc_skinny(uint64_t M, uint64_t N) { return M * N <= 32768 || N < 16 || M < 4; }
+
 int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap) {
   int cls = M <= 16 ? 2 : (M <= 32 ? 1 : 0);
   while (cls > 0 && popc_stage_smem(cls, wa, wb, kGroupKC) > smem_cap) cls--;
@@ -273,7 +312,7 @@ int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap) {
 
 cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t s) {
   if (g.M == 0 || g.N == 0) return cudaSuccess;
-  const bool skinny = g.tile_cls < 0 && ((g.M * g.N <= 32768) || g.N < 16 || g.M < 4);
+  const bool skinny = g.tile_cls < 0 && popc_skinny(g.M, g.N);
   if (skinny) {
     const uint64_t threads = g.M * g.N * 32;
     gemm_popc_skinny<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(g, e);

@@ -42,6 +42,10 @@ struct gbs_group {
   cudaGraphExec_t exec = nullptr;
   gbs::TcgPlan tc;  // problems on the tensor-core kernel
   std::vector<char> is_tc;  // per problem: on the tensor-core kernel
+  // with both kernel types, the tensor-core kernel runs on a stream forked
+  // from the caller's (and joined back), so the two share the SMs
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   uint64_t launches_per_replay = 0;
   uint32_t popc_tiles = 0;
 };
@@ -63,6 +67,9 @@ bool device_ptr(const void *p) {
 
 void free_group(gbs_group *g) {
   tcg_plan_free(&g->tc);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->join) cudaEventDestroy(g->join);
+  if (g->side) cudaStreamDestroy(g->side);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   if (g->d_probs) cudaFree(g->d_probs);
@@ -129,6 +136,14 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
 
 cudaError_t enqueue_gemm(gbs_group *g, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
+  const bool both = g->popc_tiles && g->tc.ntiles;
+  if (both) {  // the tensor-core kernel on the side stream
+    e = cudaEventRecord(g->fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(g->side, g->fork, 0);
+    if (e == cudaSuccess) e = tcg_gemm(g->tc, g->d_scratch + 2, g->side);
+    if (e == cudaSuccess) e = cudaEventRecord(g->join, g->side);
+    if (e != cudaSuccess) return e;
+  }
   if (g->popc_tiles) {
     e = cudaMemsetAsync(g->d_scratch, 0, sizeof(uint32_t), s);  // tile counter only
     if (e == cudaSuccess && g->nrs) e = launch_rowsum_grouped(g->d_rs_jobs, g->nrs, g->rs_warps, s);
@@ -136,7 +151,11 @@ cudaError_t enqueue_gemm(gbs_group *g, cudaStream_t s) {
       e = launch_gemm_popc_grouped(g->d_probs, (int)g->ctxs.size(), g->d_tiles, g->popc_tiles, g->d_scratch,
                                    g->d_scratch + 1, g->smem, g->grid, s);
   }
-  if (e == cudaSuccess) e = tcg_gemm(g->tc, g->d_scratch + 2, s);
+  if (both) {
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g->join, 0);
+  } else if (e == cudaSuccess) {
+    e = tcg_gemm(g->tc, g->d_scratch + 2, s);
+  }
   return e;
 }
 
@@ -222,16 +241,29 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
     P.neg_j = e.neg_j;
     P.shift = e.shift;
     P.c0 = e.c0;
-    P.cls = popc_tile_class(P.M, P.wa, P.wb, kGroupSmemCap);
-    smem = std::max(smem, popc_stage_smem(P.cls, P.wa, P.wb, kGroupKC));
-    probs.push_back(P);
-    const uint64_t bm = tile_bm(P.cls), bn = tile_bn(P.cls);
-    const uint64_t mt = (P.M + bm - 1) / bm, nt = (P.N + bn - 1) / bn;
-    for (uint64_t i = 0; i < mt; i++)
-      for (uint64_t j = 0; j < nt; j++) {
-        tiles.push_back(GroupTile{(uint32_t)p, (uint32_t)i, (uint32_t)j, (uint32_t)P.cls});
-        cost.push_back((uint64_t)P.wa * P.wb * P.wpr);
+    // kSkinnyTile outputs per tile, a warp each, where every BM x BN class would
+    // leave most of its tile empty: fewer than 16 rhs rows (the classes' BN is
+    // 64 or more), or a tiny output
+    if (P.N < 16 || P.M * P.N <= 4096) {
+      P.cls = kSkinnyCls;
+      probs.push_back(P);
+      const uint64_t nt = (P.M * P.N + kSkinnyTile - 1) / kSkinnyTile;
+      for (uint64_t i = 0; i < nt; i++) {
+        tiles.push_back(GroupTile{(uint32_t)p, (uint32_t)i, 0u, (uint32_t)kSkinnyCls});
+        cost.push_back(std::max<uint64_t>(1, (uint64_t)P.wa * P.wb * P.wpr / 512));
       }
+    } else {
+      P.cls = popc_tile_class(P.M, P.wa, P.wb, kGroupSmemCap);
+      smem = std::max(smem, popc_stage_smem(P.cls, P.wa, P.wb, kGroupKC));
+      probs.push_back(P);
+      const uint64_t bm = tile_bm(P.cls), bn = tile_bn(P.cls);
+      const uint64_t mt = (P.M + bm - 1) / bm, nt = (P.N + bn - 1) / bn;
+      for (uint64_t i = 0; i < mt; i++)
+        for (uint64_t j = 0; j < nt; j++) {
+          tiles.push_back(GroupTile{(uint32_t)p, (uint32_t)i, (uint32_t)j, (uint32_t)P.cls});
+          cost.push_back((uint64_t)P.wa * P.wb * P.wpr);
+        }
+    }
     if (e.ra || e.rb) {  // bipolar x regular: row sums of the regular operand
       const Mat &reg = c->lhs.bipolar() ? c->rhs : c->lhs;
       PackJob j;
@@ -269,6 +301,9 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
   if (e == cudaSuccess) e = dev_alloc((void **)&g->d_scratch, 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemset(g->d_scratch, 0, 3 * sizeof(uint32_t));
   if (e == cudaSuccess) e = prepare_gemm_popc_grouped(smem);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     cudaGetLastError();
     free_group(g);
@@ -321,6 +356,8 @@ int gbs_group_gemm(gbs_group *g, void *stream) {
 int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *const *rhs_srcs, const int *dtypes,
                       void *stream) {
   if (!g) return fail(GBS_EINVAL, "gbs_group_capture: group is NULL");
+  if (!stream)  // CUDA cannot capture the legacy default stream
+    return fail(GBS_EINVAL, "gbs_group_capture: capture needs a created stream, not the legacy default stream");
   const bool with_pack = lhs_srcs && rhs_srcs;
   if (with_pack) {
     int rc = build_pack_jobs(g, lhs_srcs, rhs_srcs, dtypes);

@@ -149,6 +149,8 @@ struct gbs_ctx {
   cudaEvent_t ev_chunk[8] = {};
   cudaEvent_t ev_packed[2] = {};
   bool ev_packed_set[2] = {false, false};
+  void *thr_stage[2] = {nullptr, nullptr};  // device copies of host-side quantisation thresholds
+  size_t thr_bytes[2] = {0, 0};
   int device = 0;
   int pipe = GBS_PIPE_AUTO;
   int variant = -1;  // pipe variant: CUDA-core tile class (0..2) or tensor-core N tile (128/256); -1 = built-in rule
@@ -183,6 +185,9 @@ cudaError_t dev_alloc(void **p, size_t bytes);
 
 // kernels (gbs_pack.cu)
 cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major, cudaStream_t s);
+// threshold-quantising import (importRegularAndQuantize); dtype GBS_I8..GBS_F32, thr [nthres][nrows]
+cudaError_t launch_pack_quantize(const Mat &m, const void *src, const void *thr, int nthres, int dtype,
+                                 int col_major, uint8_t *digits, const uint32_t *dtab, cudaStream_t s);
 // units of the row-major pack kernels: 1024-column segments per row
 inline uint64_t pack_segs_per_row(uint64_t wpr) { return (wpr * 64 + 1023) / 1024; }
 // row-major pack of padded rows [r0, r1); with digits set also the e4m3 digit rows (table dtab[4])
@@ -194,6 +199,10 @@ cudaError_t launch_export(const Mat &m, int32_t *dst, cudaStream_t s);
 // forward kernels
 cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t s);
 int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap);
+// small-output shapes (matrix-vector and the like): one warp per output
+bool popc_skinny(uint64_t M, uint64_t N);
+constexpr int kSkinnyCls = 3;    // grouped tile class of kSkinnyTile outputs, one per warp
+constexpr int kSkinnyTile = 8;
 size_t popc_stage_smem(int cls, int wa, int wb, int kc);
 constexpr int kGroupKC = 8;
 cudaError_t prepare_gemm_popc_grouped(size_t smem);

@@ -147,6 +147,71 @@ __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ sr
             warp % segs, threadIdx.x & 31);
 }
 
+// ---------------------------------------------------------------- threshold quantisation
+// importRegularAndQuantize<T> (gemmbitserial.hpp:282-305): element x of row r
+// becomes the index of the first threshold thr[t * nrows + r] with x <= thr
+// (compared in T), or nthres when x exceeds them all; with no thresholds the
+// element keeps its own value.  The low byte of that code is the code the
+// planes store (the (uint8_t) cast of :298).  For float input without
+// thresholds the float is truncated toward zero to an integer first.
+template <typename T>
+__device__ __forceinline__ uint32_t own_code(T x) {
+  return (uint32_t)(int64_t)x & 0xFFu;
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t threshold_code(T x, const T *__restrict__ thr, int nthres, uint64_t r,
+                                                   uint64_t nrows) {
+  if (nthres == 0) return own_code(x);
+  int t = 0;
+  for (; t < nthres; t++)
+    if (x <= thr[(uint64_t)t * nrows + r]) break;
+  return (uint32_t)t & 0xFFu;
+}
+
+// Row-major: a warp per 1024-column segment of a padded row, lane = 32
+// columns.  Column-major (matrix[c * nrows + r]): a warp per 32 x 32 block,
+// lane = row, so the lanes' loads of one column are contiguous.  Either way a
+// lane ends up with 32 consecutive columns of one row and stores them like
+// the regular import (planes, and digits when requested).
+template <typename T>
+__global__ void __launch_bounds__(256) pack_quantize_kernel(const T *__restrict__ src, const T *__restrict__ thr,
+                                                            int nthres, int nbits, uint64_t nrows, uint64_t ncols,
+                                                            uint64_t nrows_a, uint64_t wpr, int col_major,
+                                                            uint64_t *__restrict__ planes,
+                                                            uint8_t *__restrict__ digits, uint4 dtab) {
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  uint64_t r, col0;
+  if (!col_major) {
+    const uint64_t segs = segs_per_row(wpr);
+    if (warp >= nrows_a * segs) return;
+    r = warp / segs;
+    col0 = (warp % segs) * kSegCols + (uint64_t)lane * 32;
+  } else {
+    const uint64_t cblocks = wpr * 2;
+    if (warp >= (nrows_a / 32) * cblocks) return;
+    r = (warp / cblocks) * 32 + lane;
+    col0 = (warp % cblocks) * 32;
+  }
+  if (col0 >= wpr * 64) return;
+  uint32_t q[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) q[i] = 0u;
+  if (r < nrows) {
+#pragma unroll 4
+    for (int j = 0; j < 32; j++) {
+      const uint64_t c = col0 + j;
+      if (c < ncols) {
+        const T x = src[col_major ? c * nrows + r : r * ncols + c];
+        q[j >> 2] |= threshold_code(x, thr, nthres, r, nrows) << (8 * (j & 3));
+      }
+    }
+  }
+  emit_planes32(nbits, nrows_a, wpr, planes, r, col0, q);
+  if (digits) write_digits32(digits, nbits, nrows, ncols, wpr, dtab, r, col0, q);
+}
+
 // Index of the job owning global warp w: the last job with warp0 <= w.
 __device__ __forceinline__ int find_job(const PackJob *jobs, int njobs, uint64_t w) {
   int lo = 0, hi = njobs - 1;
@@ -313,6 +378,27 @@ cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t 
   pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
                                                           m.nrows_a, m.wpr(), vec, m.planes, r0, r1 - r0,
                                                           digits, tab);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_quantize(const Mat &m, const void *src, const void *thr, int nthres, int dtype,
+                                 int col_major, uint8_t *digits, const uint32_t *dtab, cudaStream_t s) {
+  if (m.nrows_a == 0 || m.wpr() == 0) return cudaSuccess;
+  const uint64_t warps = col_major ? (m.nrows_a / 32) * m.wpr() * 2 : m.nrows_a * segs_per_row(m.wpr());
+  const unsigned blocks = blocks_for(warps * 32, 256);
+  const uint4 tab = dtab ? make_uint4(dtab[0], dtab[1], dtab[2], dtab[3]) : make_uint4(0u, 0u, 0u, 0u);
+#define GBS_QLAUNCH(T)                                                                                              \
+  pack_quantize_kernel<T><<<blocks, 256, 0, s>>>((const T *)src, (const T *)thr, nthres, (int)m.nbits, m.nrows,      \
+                                                 m.ncols, m.nrows_a, m.wpr(), col_major, m.planes, digits, tab)
+  switch (dtype) {
+    case GBS_I8: GBS_QLAUNCH(int8_t); break;
+    case GBS_U8: GBS_QLAUNCH(uint8_t); break;
+    case GBS_I16: GBS_QLAUNCH(int16_t); break;
+    case GBS_I32: GBS_QLAUNCH(int32_t); break;
+    default: GBS_QLAUNCH(float); break;
+  }
+#undef GBS_QLAUNCH
   count_launch();
   return cudaGetLastError();
 }

@@ -83,6 +83,18 @@ WORKLOADS = {
 }
 
 
+# The reference's CaffeNet chain (benchmark.cpp:174-237): (M, K, N) of its 8
+# GEMMs (conv layers as GEMMs, then the fully connected layers as GEMVs), all
+# 2-bit unsigned weights (lhs) x 2-bit unsigned activations (rhs).
+CAFFENET = [(96, 363, 3025), (256, 2400, 729), (384, 2304, 169), (384, 3456, 169),
+            (256, 3456, 169), (4096, 9216, 1), (4096, 4096, 1), (1000, 4096, 1)]
+
+
+def caffenet_mix():
+    """The CaffeNet chain as a problem mix: (M, K, N, wA, encA, wB, encB)."""
+    return [(M, K, N, 2, "u", 2, "u") for (M, K, N) in CAFFENET]
+
+
 def workload(name: str, seed_index: int = 0):
     """Return (M, K, N, wA, sA, wB, sB, A, B) for a named workload; A is M x K, B is N x K (int8)."""
     M, K, N, (wA, eA), (wB, eB) = WORKLOADS[name]

@@ -50,7 +50,7 @@ enum {
  * x>0 to +1 and everything else to -1, other matrices keep the low nbits bits
  * of x (two's complement).  GBS_U8 follows the reference's non-template
  * uint8_t overload (gemmbitserial.hpp:249): raw low bits for every encoding. */
-enum { GBS_I8 = 0, GBS_U8 = 1, GBS_I16 = 2, GBS_I32 = 3 };
+enum { GBS_I8 = 0, GBS_U8 = 1, GBS_I16 = 2, GBS_I32 = 3, GBS_F32 = 4 /* gbs_import_quantize only */ };
 
 enum { GBS_LHS = 0, GBS_RHS = 1 };
 
@@ -111,6 +111,20 @@ GBS_API int gbs_ctx_get_info(const gbs_ctx *ctx, gbs_ctx_info *info);
  * device first.  The packing runs on `stream`; with host src the call returns
  * once src may be reused. */
 GBS_API int gbs_import(gbs_ctx *ctx, int side, const void *src, int dtype, int col_major, void *stream);
+
+/* Replaces BitSerialMatrix::importRegularAndQuantize<T> (gemmbitserial.hpp:
+ * 282-305) for one side: element x of row r becomes the index t of the first
+ * threshold thresholds[t * rows + r] with x <= threshold, or nthres when x
+ * exceeds them all (no thresholds: the element's own low byte); the low nbits
+ * bits of that index are stored.  Thresholds are [nthres][rows], of the same
+ * element type as src (GBS_I8, GBS_U8, GBS_I16, GBS_I32 or GBS_F32), sorted
+ * ascending per row as the reference assumes (unsorted ones give the
+ * reference's first-crossing result).  Only unsigned matrices: GBS_EINVAL for
+ * a signed one, where the reference asserts.  src and thresholds may be host
+ * or device memory; with host memory the call returns once both may be
+ * reused.  Float input without thresholds is truncated toward zero first. */
+GBS_API int gbs_import_quantize(gbs_ctx *ctx, int side, const void *src, const void *thresholds, int nthres,
+                                int dtype, int col_major, void *stream);
 
 /* Replaces gemmBitSerial / gemmBitSerial_generic (arch-generic.hpp:331-345,
  * macro gemmbitserial.hpp:476): res = lhs * rhs^T in the transposed layout
@@ -208,7 +222,8 @@ GBS_API int gbs_group_gemm(gbs_group *g, void *stream);
 /* Captures [grouped import of the given sources] + grouped GEMM into a CUDA
  * graph held by the group (sources NULL: GEMM only, operands already
  * imported).  The captured sources are fixed; refill their contents and
- * replay. */
+ * replay.  `stream` must be a created stream (GBS_EINVAL for NULL: CUDA
+ * cannot capture the legacy default stream). */
 GBS_API int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *const *rhs_srcs,
                               const int *dtypes, void *stream);
 

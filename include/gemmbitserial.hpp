@@ -33,6 +33,10 @@ template <typename T> struct elem;
 template <> struct elem<int8_t> { static const int code = GBS_I8; };
 template <> struct elem<int16_t> { static const int code = GBS_I16; };
 template <> struct elem<int32_t> { static const int code = GBS_I32; };
+// element types of importRegularAndQuantize<T>, which also takes uint8_t and float
+template <typename T> struct qelem { static const int code = elem<T>::code; };
+template <> struct qelem<uint8_t> { static const int code = GBS_U8; };
+template <> struct qelem<float> { static const int code = GBS_F32; };
 }  // namespace detail
 
 class BitSerialMatrix {
@@ -88,6 +92,14 @@ class BitSerialMatrix {
   // The uint8_t overload (reference gemmbitserial.hpp:249): raw low bits.
   void importRegular(uint8_t *matrix, bool readColMajor = false) {
     detail::check(gbs_import(ctx_, side_, matrix, GBS_U8, readColMajor ? 1 : 0, nullptr));
+  }
+
+  // importRegularAndQuantize<T> (reference gemmbitserial.hpp:282-305):
+  // thresholds[nThres][nrows], sorted per row; unsigned matrices only.
+  template <typename T>
+  void importRegularAndQuantize(T *matrix, T *thresholds, int nThres, bool readColMajor = false) {
+    detail::check(gbs_import_quantize(ctx_, side_, matrix, thresholds, nThres, detail::qelem<T>::code,
+                                      readColMajor ? 1 : 0, nullptr));
   }
 
   // exportRegular<T> (reference gemmbitserial.hpp:313-333) into host memory.

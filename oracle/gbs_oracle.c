@@ -26,7 +26,7 @@
 #define ORC_EXPORT __attribute__((visibility("default")))
 
 /* Input element types accepted by the import routine. */
-enum { ORC_I8 = 0, ORC_U8 = 1, ORC_I16 = 2, ORC_I32 = 3 };
+enum { ORC_I8 = 0, ORC_U8 = 1, ORC_I16 = 2, ORC_I32 = 3, ORC_F32 = 4 };
 
 typedef struct {
   int issigned;
@@ -186,6 +186,51 @@ static void mat_import(orc_matrix *m, const void *src, int dtype, int colmajor) 
 
 ORC_EXPORT void orc_import(orc_ctx *c, int side, const void *src, int dtype, int colmajor) {
   mat_import(side ? &c->rhs : &c->lhs, src, dtype, colmajor);
+}
+
+/* gemmbitserial.hpp:282-305 importRegularAndQuantize<T>: element x of row r
+ * becomes the index t of the first threshold thresholds[t*nrows + r] with
+ * x <= threshold (compared in T), or nThres when x exceeds every threshold;
+ * with nThres == 0 the loop never runs and x keeps its own value.  The
+ * (uint8_t) cast of :298 then keeps the low byte, of which the low nbits bits
+ * are stored.  For float input with nThres == 0 the cast is taken as
+ * truncation toward zero to an integer, then the low byte (C leaves float to
+ * uint8_t undefined outside [0, 256)). */
+static uint8_t quantize_code(const void *src, const void *thr, int nthres, int dtype, uint64_t idx, uint64_t r,
+                             uint64_t nrows) {
+  if (dtype == ORC_F32) {
+    const float x = ((const float *)src)[idx];
+    if (nthres == 0) return (uint8_t)(int64_t)x;
+    for (int t = 0; t < nthres; t++)
+      if (x <= ((const float *)thr)[(uint64_t)t * nrows + r]) return (uint8_t)t;
+    return (uint8_t)nthres;
+  }
+  const int64_t x = load_elem(src, dtype, idx);
+  if (nthres == 0) return (uint8_t)x;
+  for (int t = 0; t < nthres; t++)
+    if (x <= load_elem(thr, dtype, (uint64_t)t * nrows + r)) return (uint8_t)t;
+  return (uint8_t)nthres;
+}
+
+static void mat_import_quantize(orc_matrix *m, const void *src, const void *thr, int nthres, int dtype,
+                                int colmajor) {
+  memset(m->data, 0, m->nbits * mat_wpp(m) * sizeof(uint64_t));
+  for (uint64_t r = 0; r < m->nrows; r++)
+    for (uint64_t col = 0; col < m->ncols; col++) {
+      uint64_t idx = colmajor ? col * m->nrows + r : r * m->ncols + col;
+      uint8_t q = quantize_code(src, thr, nthres, dtype, idx, r, m->nrows);
+      for (uint64_t b = 0; b < m->nbits; b++)
+        if ((q >> b) & 1u) mat_row(m, b, r)[col >> 6] |= (uint64_t)1 << (col & 63);
+    }
+}
+
+/* Returns -1 for a signed matrix: the reference asserts !issigned (:283). */
+ORC_EXPORT int orc_import_quantize(orc_ctx *c, int side, const void *src, const void *thr, int nthres, int dtype,
+                                   int colmajor) {
+  orc_matrix *m = side ? &c->rhs : &c->lhs;
+  if (m->issigned) return -1;
+  mat_import_quantize(m, src, thr, nthres, dtype, colmajor);
+  return 0;
 }
 
 /* gemmbitserial.hpp:313-333 exportRegular */

@@ -25,7 +25,7 @@ REF_SO = os.path.join(HERE, "_ref", "libgbsref.so")
 
 DT_I8, DT_U8, DT_I16, DT_I32 = 0, 1, 2, 3
 _NP2DT = {np.dtype(np.int8): DT_I8, np.dtype(np.uint8): DT_U8,
-          np.dtype(np.int16): DT_I16, np.dtype(np.int32): DT_I32}
+          np.dtype(np.int16): DT_I16, np.dtype(np.int32): DT_I32, np.dtype(np.float32): 4}
 
 _lib = None
 _ref = None
@@ -57,6 +57,7 @@ def lib():
         L.orc_res.argtypes = [vp]
         L.orc_import.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int]
         L.orc_export.argtypes = [vp, C.c_int, vp]
+        L.orc_import_quantize.argtypes = [vp, C.c_int, vp, vp, C.c_int, C.c_int, C.c_int]
         L.orc_sum_rows.argtypes = [vp, C.c_int, vp]
         L.orc_gemm.argtypes = [vp]
         L.orc_gemm_threads.argtypes = [vp, C.c_int]
@@ -77,6 +78,7 @@ def ref():
                               vp, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp, vp]
         R.ref_sum_rows.argtypes = [u64, u64, u64, C.c_int, vp, C.c_int, vp]
         R.ref_roundtrip.argtypes = [u64, u64, u64, C.c_int, vp, C.c_int, vp]
+        R.ref_quantize_export.argtypes = [u64, u64, u64, vp, vp, C.c_int, C.c_int, C.c_int, vp]
         R.ref_time_gemm.restype = C.c_double
         R.ref_time_gemm.argtypes = [u64, u64, u64, u64, u64, C.c_int, C.c_int,
                                     vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp]
@@ -101,6 +103,16 @@ class OracleContext:
     def import_(self, side: int, arr: np.ndarray, colmajor: bool = False):
         arr = np.ascontiguousarray(arr)
         lib().orc_import(self.h, side, _ptr(arr), _NP2DT[arr.dtype], int(colmajor))
+
+    def import_quantize(self, side: int, arr: np.ndarray, thresholds: np.ndarray, colmajor: bool = False):
+        """importRegularAndQuantize (gemmbitserial.hpp:282-305); thresholds shaped [nThres][nrows]."""
+        arr = np.ascontiguousarray(arr)
+        thr = np.ascontiguousarray(thresholds, dtype=arr.dtype)
+        nthres = int(thr.shape[0]) if thr.ndim == 2 else 0
+        rc = lib().orc_import_quantize(self.h, side, _ptr(arr), _ptr(thr) if thr.size else None, nthres,
+                                       _NP2DT[arr.dtype], int(colmajor))
+        if rc != 0:
+            raise ValueError("threshold quantization needs an unsigned matrix")
 
     def gemm(self, threads: int = 1):
         if threads > 1:
@@ -207,3 +219,27 @@ def adjoint_fp64(dC: np.ndarray, Avals: np.ndarray, Bvals: np.ndarray):
     dA = d.T @ Bvals.astype(np.float64)
     dB = d @ Avals.astype(np.float64)
     return dA, dB
+
+
+def quantize_values(arr: np.ndarray, thresholds: np.ndarray, bits: int, colmajor: bool = False) -> np.ndarray:
+    """The values an unsigned ``bits``-bit matrix holds after importRegularAndQuantize of ``arr``
+    (rows x cols, or cols x rows when ``colmajor``) with thresholds [nThres][rows]."""
+    rows, cols = (arr.shape[1], arr.shape[0]) if colmajor else arr.shape
+    ctx = OracleContext(rows, cols, 1, bits, 1, False, False)
+    ctx.import_quantize(0, arr, thresholds, colmajor)
+    out = np.zeros((rows, cols), np.int32)
+    if rows * cols:
+        lib().orc_export(ctx.h, 0, _ptr(out))
+    return out
+
+
+def ref_quantize_values(arr: np.ndarray, thresholds: np.ndarray, bits: int, colmajor: bool = False) -> np.ndarray:
+    """The same through the compiled reference (oracle/_ref)."""
+    arr = np.ascontiguousarray(arr)
+    thr = np.ascontiguousarray(thresholds, dtype=arr.dtype)
+    rows, cols = (arr.shape[1], arr.shape[0]) if colmajor else arr.shape
+    out = np.zeros((rows, cols), np.int32)
+    nthres = int(thr.shape[0]) if thr.ndim == 2 else 0
+    ref().ref_quantize_export(rows, cols, bits, _ptr(arr), _ptr(thr) if thr.size else None, nthres,
+                              _NP2DT[arr.dtype], int(colmajor), _ptr(out))
+    return out

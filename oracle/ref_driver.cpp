@@ -5,8 +5,8 @@
 // into oracle/_ref/libgbsref.so by oracle/Makefile.  It exists where the
 // reference sources exist and is used to pin the C restatement in
 // gbs_oracle.c and to generate golden vectors.  It calls only the reference's
-// public API: allocGEMMContext, importRegular, gemmBitSerial, sumRows,
-// exportRegular and deallocGEMMContext.
+// public API: allocGEMMContext, importRegular, importRegularAndQuantize,
+// gemmBitSerial, sumRows, exportRegular and deallocGEMMContext.
 #include <stdint.h>
 #include <string.h>
 #include <chrono>
@@ -17,7 +17,7 @@
 using namespace gemmbitserial;
 
 namespace {
-enum { I8 = 0, U8 = 1, I16 = 2, I32 = 3 };
+enum { I8 = 0, U8 = 1, I16 = 2, I32 = 3, F32 = 4 };
 
 void do_import(BitSerialMatrix &m, const void *src, int dtype, bool colmajor) {
   switch (dtype) {
@@ -72,6 +72,23 @@ int ref_roundtrip(uint64_t rows, uint64_t cols, uint64_t bits, int sgn, const vo
                   int32_t *out) {
   BitSerialMatrix bsm = BitSerialMatrix::alloc(bits, rows, cols, sgn != 0);
   do_import(bsm, src, dt, false);
+  bsm.exportRegular(out);
+  BitSerialMatrix::dealloc(bsm);
+  return 0;
+}
+
+// importRegularAndQuantize into an unsigned matrix, then exportRegular.
+int ref_quantize_export(uint64_t rows, uint64_t cols, uint64_t bits, const void *src, const void *thr, int nthres,
+                        int dt, int colmajor, int32_t *out) {
+  BitSerialMatrix bsm = BitSerialMatrix::alloc(bits, rows, cols, false);
+  const bool cm = colmajor != 0;
+  switch (dt) {
+    case I8: bsm.importRegularAndQuantize((int8_t *)src, (int8_t *)thr, nthres, cm); break;
+    case U8: bsm.importRegularAndQuantize((uint8_t *)src, (uint8_t *)thr, nthres, cm); break;
+    case I16: bsm.importRegularAndQuantize((int16_t *)src, (int16_t *)thr, nthres, cm); break;
+    case I32: bsm.importRegularAndQuantize((int32_t *)src, (int32_t *)thr, nthres, cm); break;
+    default: bsm.importRegularAndQuantize((float *)src, (float *)thr, nthres, cm); break;
+  }
   bsm.exportRegular(out);
   BitSerialMatrix::dealloc(bsm);
   return 0;

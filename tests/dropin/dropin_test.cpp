@@ -169,6 +169,54 @@ int main() {
     failed += report("aliasing copies", memcmp(v[0].res, want.data(), want.size() * 4) == 0, 1);
     deallocGEMMContext(copy);
   }
+  {  // threshold-quantised import (importRegularAndQuantize) feeding a GEMM, float and int16 input
+    int ok = 0, total = 0;
+    for (int d : {7, 32, 100})
+      for (int nthres : {0, 1, 3}) {
+        const int M = d, K = 2 * d + 5, N = d + 3, wA = 2;
+        std::vector<float> af(M * K);
+        std::vector<int16_t> ai(M * K);
+        for (int i = 0; i < M * K; i++) {
+          af[i] = (float)(next_u64() % 1000) / 100.f;  // [0, 10)
+          ai[i] = (int16_t)(next_u64() % 2000) - 1000;
+        }
+        std::vector<float> tf(nthres * M);
+        std::vector<int16_t> ti(nthres * M);
+        for (int r = 0; r < M; r++)
+          for (int t = 0; t < nthres; t++) {  // ascending per row
+            tf[t * M + r] = 2.5f * (t + 1) + (float)(r % 3);
+            ti[t * M + r] = (int16_t)(300 * t - 400 + r);
+          }
+        std::vector<int8_t> bt(N * K);
+        fill(bt, 2, false);
+        for (int v = 0; v < 2; v++) {
+          std::vector<uint8_t> q(M * K);  // the reference's loop: first threshold crossed, else nThres
+          for (int r = 0; r < M; r++)
+            for (int c = 0; c < K; c++) {
+              int idx = r * K + c, t = 0;
+              if (nthres == 0) {
+                q[idx] = v ? (uint8_t)ai[idx] : (uint8_t)af[idx];
+                continue;
+              }
+              for (; t < nthres; t++)
+                if (v ? ai[idx] <= ti[t * M + r] : af[idx] <= tf[t * M + r]) break;
+              q[idx] = (uint8_t)t;
+            }
+          for (auto &x : q) x &= (1 << wA) - 1;
+          std::vector<int32_t> want(M * N);
+          naive(q, bt, want, M, K, N);
+          GEMMContext ctx = allocGEMMContext(M, K, N, wA, 2, false, false);
+          if (v) ctx.lhs.importRegularAndQuantize(ai.data(), ti.data(), nthres);
+          else ctx.lhs.importRegularAndQuantize(af.data(), tf.data(), nthres);
+          ctx.rhs.importRegular(bt.data());
+          gemmBitSerial(ctx);
+          ok += memcmp(ctx.res, want.data(), M * N * 4) == 0;
+          total++;
+          deallocGEMMContext(ctx);
+        }
+      }
+    failed += report("threshold-quantised import", ok, total);
+  }
   printf(failed ? "Some tests failed\n" : "All tests completed successfully\n");
   return failed;
 }

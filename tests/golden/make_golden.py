@@ -18,6 +18,11 @@ Writes
                      out-of-range values, odd shapes, K not a multiple of 64).
   ref_configs.json-- sha256 of the reference's int32 results on the full-size
                      benchmark workloads (seeded by gemmbitserial_gb300.datagen).
+  ref_quantize.npz -- importRegularAndQuantize (gemmbitserial.hpp:282-305) through
+                     the reference, then exportRegular: inputs, thresholds
+                     [nThres][rows] and the resulting values, for every element
+                     type, sorted and unsorted thresholds, no thresholds, more
+                     levels than the bit width holds, and column-major input.
 """
 from __future__ import annotations
 
@@ -146,6 +151,41 @@ def make_vectors() -> None:
         json.dump({"gemm": meta, "rows": rows}, f, separators=(",", ":"))
 
 
+QUANTIZE_CASES = [  # rows, cols, bits, nThres, sorted thresholds, column-major
+    (5, 70, 2, 3, True, False), (17, 130, 3, 7, True, True), (8, 64, 2, 7, True, False),
+    (9, 33, 4, 0, True, False), (4, 100, 1, 1, False, False), (6, 77, 3, 5, False, True),
+    (1, 1, 2, 2, True, False), (33, 65, 8, 20, True, False), (64, 300, 4, 15, True, False),
+    (40, 257, 2, 3, True, True),
+]
+
+
+def make_quantize() -> None:
+    out = {}
+    dts = [np.int8, np.uint8, np.int16, np.int32, np.float32]
+    for i, (rows, cols, bits, nthres, srt, cm) in enumerate(QUANTIZE_CASES):
+        for dt in dts:
+            rng = np.random.default_rng(1000 * i + dts.index(dt))
+            if dt == np.float32:
+                a = rng.normal(0, 3, (rows, cols)).astype(dt)
+                if nthres == 0:  # (uint8_t)float is only defined for values in [0, 256)
+                    a = rng.integers(0, 256, (rows, cols)).astype(dt)
+                t = rng.normal(0, 3, (nthres, rows)).astype(dt)
+            else:
+                info = np.iinfo(dt)
+                lo, hi = max(int(info.min), -1000), min(int(info.max), 1000)
+                a = rng.integers(lo, hi + 1, (rows, cols)).astype(dt)
+                t = rng.integers(lo, hi + 1, (nthres, rows)).astype(dt)
+            if srt:
+                t = np.sort(t, axis=0)
+            src = np.ascontiguousarray(a.T) if cm else a
+            key = f"q{i}_{np.dtype(dt).name}"
+            out[key + "_src"] = src
+            out[key + "_thr"] = t
+            out[key + "_meta"] = np.array([rows, cols, bits, nthres, int(cm)], np.int64)
+            out[key + "_values"] = O.ref_quantize_values(src, t, bits, cm)
+    np.savez_compressed(os.path.join(HERE, "ref_quantize.npz"), **out)
+
+
 def make_config_hashes() -> None:
     res = {}
     for name in datagen.WORKLOADS:
@@ -164,5 +204,6 @@ if __name__ == "__main__":
         O.build(ref=True)
     make_mnist(refdir)
     make_vectors()
+    make_quantize()
     make_config_hashes()
     print("golden fixtures written to", HERE)

@@ -194,6 +194,18 @@ def test_grouped_rejects_bad_descriptors_without_faulting(lib):
             deallocGEMMContext(c)
 
 
+def test_grouped_capture_rejects_the_legacy_stream(lib):
+    mix = [(40, 640, 300, 2, "u", 3, "s")]
+    ctxs = make_contexts(mix)
+    g = Group(ctxs)
+    try:
+        assert lib.gbs_group_capture(g._h, None, None, None, None) == _capi.GBS_EINVAL
+        assert b"legacy default stream" in lib.gbs_last_error()
+    finally:
+        g.free()
+        deallocGEMMContext(ctxs[0])
+
+
 def test_grouped_rejects_host_sources():
     mix = [(4, 64, 4, 1, "u", 1, "u")]
     ctxs = make_contexts(mix)
@@ -209,3 +221,37 @@ def test_grouped_rejects_host_sources():
     finally:
         g.free()
         deallocGEMMContext(ctxs[0])
+
+
+def test_caffenet_chain_as_a_group():
+    """The reference's CaffeNet chain (benchmark.cpp:174-237): 8 GEMMs / GEMVs, 2-bit x 2-bit
+    unsigned, run as one group (and its graph); every result equals the oracle's."""
+    import torch
+    mix = datagen.caffenet_mix()
+    host = [(datagen.operand(datagen.SEED_BASE + 900 + 2 * i, M, K, wA, eA),
+             datagen.operand(datagen.SEED_BASE + 901 + 2 * i, N, K, wB, eB))
+            for i, (M, K, N, wA, eA, wB, eB) in enumerate(mix)]
+    ctxs = make_contexts(mix)
+    dev = [(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()) for A, B in host]
+    g = Group(ctxs)
+    try:
+        st = g.stats()
+        assert st["popc_problems"] + st["tc_problems"] == len(mix)
+        g.import_([a for a, _ in dev], [b for _, b in dev])
+        g.gemm()
+        torch.cuda.synchronize()
+        assert g.status() == _capi.GBS_OK
+        want = [O.oracle_gemm(A, B, 2, 2, False, False, threads=8) for A, B in host]
+        for (M, K, N, *_r), c, w in zip(mix, ctxs, want):
+            assert np.array_equal(c.res.reshape(N, M), w), (M, K, N)
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            g.capture([a for a, _ in dev], [b for _, b in dev], stream=s)
+            g.replay(stream=s)
+        s.synchronize()
+        for (M, K, N, *_r), c, w in zip(mix, ctxs, want):
+            assert np.array_equal(c.res.reshape(N, M), w), (M, K, N)
+    finally:
+        g.free()
+        for c in ctxs:
+            deallocGEMMContext(c)

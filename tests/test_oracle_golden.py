@@ -124,3 +124,30 @@ def test_oracle_matches_compiled_reference_random():
         pl = np.concatenate([ctx.planes(0).ravel(), ctx.planes(1).ravel()])
         assert np.array_equal(ctx.res(), r_ref) and ctx.dims == dims
         assert np.array_equal(pl, planes[: pl.size])
+
+
+def quantize_cases():
+    z = np.load(os.path.join(GOLD, "ref_quantize.npz"))
+    keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
+    return [(k, z[k + "_src"], z[k + "_thr"], z[k + "_meta"], z[k + "_values"]) for k in keys]
+
+
+def test_quantize_oracle_matches_reference_fixtures():
+    """importRegularAndQuantize (gemmbitserial.hpp:282-305): the C restatement against the
+    reference's own results for every element type, unsorted and empty threshold sets,
+    more levels than the width holds, and column-major input."""
+    cases = quantize_cases()
+    assert len(cases) >= 50
+    for key, src, thr, meta, want in cases:
+        rows, cols, bits, nthres, cm = (int(x) for x in meta)
+        assert thr.shape == (nthres, rows)
+        got = O.quantize_values(src, thr, bits, bool(cm))
+        assert np.array_equal(got, want), key
+        if O.ref_available():
+            assert np.array_equal(O.ref_quantize_values(src, thr, bits, bool(cm)), want), key
+
+
+def test_quantize_oracle_rejects_signed():
+    ctx = O.OracleContext(4, 64, 4, 2, 2, True, False)
+    with pytest.raises(ValueError):
+        ctx.import_quantize(0, np.zeros((4, 64), np.int8), np.zeros((1, 4), np.int8))
