@@ -36,6 +36,9 @@ SIGNATURES = {
     "gbs_ctx_get_info": (i32, [vp, C.POINTER(CtxInfo)]),
     "gbs_import": (i32, [vp, i32, vp, i32, i32, vp]),
     "gbs_import_quantize": (i32, [vp, i32, vp, vp, i32, i32, i32, vp]),
+    "gbs_get_bit": (i32, [vp, i32, u64, u64, u64, C.POINTER(i32)]),
+    "gbs_set_bit": (i32, [vp, i32, u64, u64, u64, i32]),
+    "gbs_clear": (i32, [vp, i32, vp]),
     "gbs_gemm": (i32, [vp, vp]),
     "gbs_get_result": (i32, [vp, vp, vp]),
     "gbs_sum_rows": (i32, [vp, i32, vp, vp]),

@@ -50,7 +50,7 @@ def _src(arr, allow_float: bool = False):
             dt = {torch.int8: _capi.GBS_I8, torch.uint8: _capi.GBS_U8, torch.int16: _capi.GBS_I16,
                   torch.int32: _capi.GBS_I32, torch.float32: _capi.GBS_F32}[t.dtype]
             if dt == _capi.GBS_F32 and not allow_float:
-                raise TypeError("float input is accepted by importRegularAndQuantize only")
+                raise TypeError("float input is not accepted here")
             return C.c_void_p(t.data_ptr()), dt, t
     except ImportError:
         pass
@@ -106,8 +106,9 @@ class BitSerialMatrix:
         return self.nrows_a * self.wordsPerRow()
 
     def importRegular(self, matrix, readColMajor: bool = False, stream=None) -> None:
-        """importRegular<T> / importRegular(uint8_t*) (gemmbitserial.hpp:213, 249)."""
-        ptr, dt, keep = _src(matrix)
+        """importRegular<T> / importRegular(uint8_t*) (gemmbitserial.hpp:213, 249); T = int8, int16,
+        int32 or float32."""
+        ptr, dt, keep = _src(matrix, allow_float=True)
         _capi.check(_capi.load().gbs_import(self._ctx._h, self._side, ptr, dt, int(bool(readColMajor)),
                                             _stream_handle(stream)))
         del keep
@@ -128,6 +129,21 @@ class BitSerialMatrix:
         _capi.check(_capi.load().gbs_import_quantize(self._ctx._h, self._side, ptr, tptr, int(nThres), dt,
                                                      int(bool(readColMajor)), _stream_handle(stream)))
         del keep, tkeep
+
+    # single bits (gemmbitserial.hpp:90-108); each call synchronises the device
+    def get(self, bit: int, row: int, col: int) -> bool:
+        v = C.c_int()
+        _capi.check(_capi.load().gbs_get_bit(self._ctx._h, self._side, bit, row, col, C.byref(v)))
+        return bool(v.value)
+
+    def set(self, bit: int, row: int, col: int) -> None:
+        _capi.check(_capi.load().gbs_set_bit(self._ctx._h, self._side, bit, row, col, 1))
+
+    def unset(self, bit: int, row: int, col: int) -> None:
+        _capi.check(_capi.load().gbs_set_bit(self._ctx._h, self._side, bit, row, col, 0))
+
+    def clearAll(self, stream=None) -> None:
+        _capi.check(_capi.load().gbs_clear(self._ctx._h, self._side, _stream_handle(stream)))
 
     def planes(self, stream=None) -> np.ndarray:
         """Host copy of the packed planes, shape [nbits, nrows_a, ncols_a/64] (uint64)."""

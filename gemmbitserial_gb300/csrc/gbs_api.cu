@@ -73,7 +73,7 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-size_t elem_size(int dtype) { return dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1; }
+size_t elem_size(int dtype) { return dtype == GBS_I16 ? 2 : (dtype == GBS_I32 || dtype == GBS_F32) ? 4 : 1; }
 
 void free_ctx_buffers(gbs_ctx *c) {
   if (c->lhs.planes) cudaFree(c->lhs.planes);
@@ -285,7 +285,7 @@ bool import_writes_digits(const gbs_ctx *c) { return effective_pipe(c) == GBS_PI
 int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, void *stream) {
   if (!c) return fail(GBS_EINVAL, "gbs_import: ctx is NULL");
   if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_import: side must be 0 (lhs) or 1 (rhs)");
-  if (dtype < GBS_I8 || dtype > GBS_I32) return fail(GBS_EINVAL, "gbs_import: unknown dtype");
+  if (dtype < GBS_I8 || dtype > GBS_F32) return fail(GBS_EINVAL, "gbs_import: unknown dtype");
   Mat &m = side ? c->rhs : c->lhs;
   const uint64_t n = m.nrows * m.ncols;
   if (n && !src) return fail(GBS_EINVAL, "gbs_import: src is NULL");
@@ -429,6 +429,74 @@ int gbs_import_quantize(gbs_ctx *c, int side, const void *src, const void *thres
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: stream sync");
   }
+  return GBS_OK;
+}
+
+namespace {
+
+// The device word holding (bit, row, col) of one side, after bounds checks.
+int bit_word(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, uint64_t **word, const char *who) {
+  if (!c) return fail(GBS_EINVAL, std::string(who) + ": ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, std::string(who) + ": bad side");
+  const Mat &m = side ? c->rhs : c->lhs;
+  if (bit >= m.nbits || row >= m.nrows_a || col >= m.ncols_a)
+    return fail(GBS_EINVAL, std::string(who) + ": bit, row or column out of range");
+  *word = m.planes + bit * m.nrows_a * m.wpr() + row * m.wpr() + (col >> 6);
+  return GBS_OK;
+}
+
+}  // namespace
+
+int gbs_get_bit(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, int *value) {
+  uint64_t *w = nullptr;
+  int rc = bit_word(c, side, bit, row, col, &w, "gbs_get_bit");
+  if (rc != GBS_OK) return rc;
+  if (!value) return fail(GBS_EINVAL, "gbs_get_bit: value is NULL");
+  DeviceGuard g(c->device);
+  uint64_t v = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_get_bit");
+  *value = (int)((v >> (col & 63)) & 1u);
+  return GBS_OK;
+}
+
+int gbs_set_bit(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, int value) {
+  uint64_t *w = nullptr;
+  int rc = bit_word(c, side, bit, row, col, &w, "gbs_set_bit");
+  if (rc != GBS_OK) return rc;
+  const Mat &mm = side ? c->rhs : c->lhs;
+  if (row >= mm.nrows || col >= mm.ncols)  // padding stays zero: results never depend on it
+    return fail(GBS_EINVAL, "gbs_set_bit: row or column in the padding");
+  DeviceGuard g(c->device);
+  uint64_t v = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) {
+    const uint64_t mask = (uint64_t)1 << (col & 63);
+    v = value ? (v | mask) : (v & ~mask);
+    e = cudaMemcpy(w, &v, sizeof(v), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_set_bit");
+  Mat &m = side ? c->rhs : c->lhs;
+  m.imported = true;
+  c->digits_valid[side] = false;  // derived operands no longer match the planes
+  c->vt_valid[side] = false;
+  return GBS_OK;
+}
+
+int gbs_clear(gbs_ctx *c, int side, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_clear: ctx is NULL");
+  if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_clear: bad side");
+  Mat &m = side ? c->rhs : c->lhs;
+  DeviceGuard g(c->device);
+  if (m.words()) {
+    cudaError_t e = cudaMemsetAsync(m.planes, 0, m.words() * 8, as_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_clear");
+  }
+  m.imported = true;
+  c->digits_valid[side] = false;
+  c->vt_valid[side] = false;
   return GBS_OK;
 }
 

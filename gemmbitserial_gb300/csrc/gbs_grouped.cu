@@ -96,7 +96,7 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
     for (int side = 0; side < 2; side++) {
       const void *src = side ? rhs[p] : lhs[p];
       const int dt = dtypes ? dtypes[2 * p + side] : GBS_I8;
-      if (dt < GBS_I8 || dt > GBS_I32) return fail(GBS_EINVAL, "gbs_group: unknown dtype");
+      if (dt < GBS_I8 || dt > GBS_F32) return fail(GBS_EINVAL, "gbs_group: unknown dtype");
       const Mat &m = side ? g->ctxs[p]->rhs : g->ctxs[p]->lhs;
       if (m.nrows_a == 0 || m.wpr() == 0) continue;
       if (m.nrows * m.ncols && (!src || !device_ptr(src)))

@@ -72,7 +72,7 @@ extern "C" int gbs_gemm_noalloc(const void *lhs, int lhs_dtype, const void *rhs,
                                 int rhsSigned, int32_t *res, void *stream) {
   if (lhsBits < 1 || lhsBits > (uint64_t)kMaxBits || rhsBits < 1 || rhsBits > (uint64_t)kMaxBits)
     return fail(GBS_EINVAL, "gbs_gemm_noalloc: bit widths must be in [1, 8]");
-  if (lhs_dtype < GBS_I8 || lhs_dtype > GBS_I32 || rhs_dtype < GBS_I8 || rhs_dtype > GBS_I32)
+  if (lhs_dtype < GBS_I8 || lhs_dtype > GBS_F32 || rhs_dtype < GBS_I8 || rhs_dtype > GBS_F32)
     return fail(GBS_EINVAL, "gbs_gemm_noalloc: unknown dtype");
   if (M > (1ull << 31) || N > (1ull << 31) || K > (1ull << 31))
     return fail(GBS_EINVAL, "gbs_gemm_noalloc: shape too large");

@@ -31,6 +31,25 @@ __device__ __forceinline__ uint32_t code_of(int64_t x, int dtype, int bipolar) {
   return (uint32_t)(x & 0xff);
 }
 
+// quantize<float> (gemmbitserial.hpp:170-186): bipolar maps x > 0 to 1; a
+// negative x of a signed matrix becomes 2^(w-1) + (uint8_t)(x + 2^(w-1)), the
+// sum taken in float; otherwise (uint8_t)x.  Float -> integer casts truncate
+// toward zero, then keep the low byte.
+__device__ __forceinline__ uint32_t code_of_f32(float x, int bipolar, int issigned, int nbits) {
+  if (bipolar) return x > 0.f ? 1u : 0u;
+  if (issigned && x < 0.f) {
+    const int64_t h = (int64_t)1 << (nbits - 1);
+    return (uint32_t)(h + (int64_t)(x + (float)h)) & 0xffu;
+  }
+  return (uint32_t)(int64_t)x & 0xffu;
+}
+
+__device__ __forceinline__ uint32_t elem_code(const void *src, int dtype, uint64_t idx, int bipolar, int issigned,
+                                              int nbits) {
+  if (dtype == GBS_F32) return code_of_f32(((const float *)src)[idx], bipolar, issigned, nbits);
+  return code_of(load_elem(src, dtype, idx), dtype, bipolar);
+}
+
 // Bits b of the four bytes of x, gathered into a nibble (byte i -> bit i).
 // (x>>b)&0x01010101 leaves one bit per byte at positions 0, 8, 16, 24; the
 // multiply by 1 + 2^7 + 2^14 + 2^21 lands them, carry-free, at 21..24.
@@ -46,9 +65,9 @@ constexpr int kSegCols = 1024;
 
 __host__ __device__ inline uint64_t segs_per_row(uint64_t wpr) { return (wpr * 64 + kSegCols - 1) / kSegCols; }
 
-__device__ __forceinline__ void load_codes32(const void *__restrict__ src, int dtype, int bipolar, uint64_t nrows,
-                                             uint64_t ncols, int vec, uint64_t r, uint64_t col0,
-                                             uint32_t (&q)[8]) {
+__device__ __forceinline__ void load_codes32(const void *__restrict__ src, int dtype, int bipolar, int issigned,
+                                             int nbits, uint64_t nrows, uint64_t ncols, int vec, uint64_t r,
+                                             uint64_t col0, uint32_t (&q)[8]) {
 #pragma unroll
   for (int i = 0; i < 8; i++) q[i] = 0u;
   if (r >= nrows || col0 >= ncols) return;
@@ -68,7 +87,7 @@ __device__ __forceinline__ void load_codes32(const void *__restrict__ src, int d
   } else {
 #pragma unroll 4
     for (int j = 0; j < 32; j++)
-      if (col0 + j < ncols) q[j >> 2] |= code_of(load_elem(src, dtype, base + j), dtype, bipolar) << (8 * (j & 3));
+      if (col0 + j < ncols) q[j >> 2] |= elem_code(src, dtype, base + j, bipolar, issigned, nbits) << (8 * (j & 3));
   }
 }
 
@@ -119,14 +138,15 @@ __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int
 }
 
 // One 1024-column unit: codes, planes and (optionally) digits of the lane's 32 columns.
-__device__ __forceinline__ void pack_unit(const void *__restrict__ src, int dtype, int bipolar, int nbits,
+__device__ __forceinline__ void pack_unit(const void *__restrict__ src, int dtype, int bipolar, int issigned,
+                                          int nbits,
                                           uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr, int vec,
                                           uint64_t *__restrict__ planes, uint8_t *__restrict__ digits, uint4 dtab,
                                           uint64_t r, uint64_t seg, int lane) {
   const uint64_t col0 = seg * kSegCols + (uint64_t)lane * 32;
   if (col0 >= wpr * 64) return;  // past the padded row
   uint32_t q[8];
-  load_codes32(src, dtype, bipolar, nrows, ncols, vec, r, col0, q);
+  load_codes32(src, dtype, bipolar, issigned, nbits, nrows, ncols, vec, r, col0, q);
   emit_planes32(nbits, nrows_a, wpr, planes, r, col0, q);
   if (digits) write_digits32(digits, nbits, nrows, ncols, wpr, dtab, r, col0, q);
 }
@@ -135,7 +155,7 @@ __device__ __forceinline__ void pack_unit(const void *__restrict__ src, int dtyp
 // set, the lanes also write the rows' e4m3 digits (the tensor-core pipe's
 // operand), from the same loads.
 __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ src, int dtype, int bipolar,
-                                                     int nbits, uint64_t nrows, uint64_t ncols,
+                                                     int issigned, int nbits, uint64_t nrows, uint64_t ncols,
                                                      uint64_t nrows_a, uint64_t wpr, int vec,
                                                      uint64_t *__restrict__ planes, uint64_t row0,
                                                      uint64_t nrows_launch, uint8_t *__restrict__ digits,
@@ -143,7 +163,8 @@ __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ sr
   const uint64_t segs = segs_per_row(wpr);
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= nrows_launch * segs) return;  // warp-uniform
-  pack_unit(src, dtype, bipolar, nbits, nrows, ncols, nrows_a, wpr, vec, planes, digits, dtab, row0 + warp / segs,
+  pack_unit(src, dtype, bipolar, issigned, nbits, nrows, ncols, nrows_a, wpr, vec, planes, digits, dtab,
+            row0 + warp / segs,
             warp % segs, threadIdx.x & 31);
 }
 
@@ -252,7 +273,8 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
         sg = local % J.segs;
       }
       const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
-      pack_unit(J.src, J.dtype, J.nbits == 1 && J.issigned, J.nbits, J.nrows, J.ncols, J.nrows_a, J.wpr, J.vec,
+      pack_unit(J.src, J.dtype, J.nbits == 1 && J.issigned, J.issigned, J.nbits, J.nrows, J.ncols, J.nrows_a, J.wpr,
+                J.vec,
                 J.planes, J.digits, tab, r, sg, lane);
     }
   }
@@ -263,7 +285,7 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
 // lane l reads column c0+l (then c0+32+l) down the 32 rows, and one ballot per
 // (row, plane) gathers 32 columns of that row.  Lane j keeps row j's word.
 __global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ src, int dtype, int bipolar,
-                                                     int nbits, uint64_t nrows, uint64_t ncols,
+                                                     int issigned, int nbits, uint64_t nrows, uint64_t ncols,
                                                      uint64_t nrows_a, uint64_t wpr,
                                                      uint64_t *__restrict__ planes) {
   const uint64_t rgroups = nrows_a / 32;
@@ -281,7 +303,7 @@ __global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ sr
     if (c < ncols) {
       for (int j = 0; j < 32; j++) {
         uint64_t r = r0 + j;
-        if (r < nrows) q[j >> 2] |= code_of(load_elem(src, dtype, c * nrows + r), dtype, bipolar) << (8 * (j & 3));
+        if (r < nrows) q[j >> 2] |= elem_code(src, dtype, c * nrows + r, bipolar, issigned, nbits) << (8 * (j & 3));
       }
     }
     for (int j = 0; j < 32; j++) {
@@ -371,11 +393,11 @@ cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t 
                              const uint32_t *dtab, cudaStream_t s) {
   if (m.nrows_a == 0 || m.wpr() == 0 || r1 <= r0) return cudaSuccess;
   const int bip = m.bipolar() ? 1 : 0;
-  const size_t esz = dtype == GBS_I16 ? 2 : dtype == GBS_I32 ? 4 : 1;
+  const size_t esz = dtype == GBS_I16 ? 2 : (dtype == GBS_I32 || dtype == GBS_F32) ? 4 : 1;
   const int vec = (esz == 1 && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0) ? 1 : 0;
   const uint64_t warps = (r1 - r0) * segs_per_row(m.wpr());
   const uint4 tab = dtab ? make_uint4(dtab[0], dtab[1], dtab[2], dtab[3]) : make_uint4(0u, 0u, 0u, 0u);
-  pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
+  pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, m.issigned, (int)m.nbits, m.nrows, m.ncols,
                                                           m.nrows_a, m.wpr(), vec, m.planes, r0, r1 - r0,
                                                           digits, tab);
   count_launch();
@@ -410,7 +432,7 @@ cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major,
     return launch_pack_rows(m, src, dtype, 0, m.nrows_a, nullptr, nullptr, s);
   } else {
     const uint64_t warps = (m.nrows_a / 32) * m.wpr();
-    pack_colmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, (int)m.nbits, m.nrows, m.ncols,
+    pack_colmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, m.issigned, (int)m.nbits, m.nrows, m.ncols,
                                                             m.nrows_a, m.wpr(), m.planes);
   }
   count_launch();

@@ -49,8 +49,12 @@ enum {
  * reference's importRegular<T> (gemmbitserial.hpp:213): bipolar matrices map
  * x>0 to +1 and everything else to -1, other matrices keep the low nbits bits
  * of x (two's complement).  GBS_U8 follows the reference's non-template
- * uint8_t overload (gemmbitserial.hpp:249): raw low bits for every encoding. */
-enum { GBS_I8 = 0, GBS_U8 = 1, GBS_I16 = 2, GBS_I32 = 3, GBS_F32 = 4 /* gbs_import_quantize only */ };
+ * uint8_t overload (gemmbitserial.hpp:249): raw low bits for every encoding.
+ * GBS_F32 follows importRegular<float> (quantize<float>, :170-186): bipolar
+ * x>0 -> +1; a negative x of a signed matrix -> 2^(w-1) + (uint8_t)(x +
+ * 2^(w-1)); otherwise (uint8_t)x, float-to-integer casts truncating toward
+ * zero (the reference defines them only for values in [0, 256)). */
+enum { GBS_I8 = 0, GBS_U8 = 1, GBS_I16 = 2, GBS_I32 = 3, GBS_F32 = 4 };
 
 enum { GBS_LHS = 0, GBS_RHS = 1 };
 
@@ -152,6 +156,19 @@ GBS_API int gbs_export(gbs_ctx *ctx, int side, int32_t *dst, void *stream);
  * nbits * nrows_a * ncols_a/64 uint64 words.  With host dst the call returns
  * after the copy has completed. */
 GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
+
+/* BitSerialMatrix::get / set / unset (gemmbitserial.hpp:90-108) on one bit
+ * of one side's device planes: bit < nbits, row < nrows_a, col < ncols_a
+ * for get, row < nrows and col < ncols for set (padding stays zero), else
+ * GBS_EINVAL (the reference does not check).  Both synchronise the
+ * device, then read or read-modify-write the one word; a set marks the side
+ * imported, so matrices can be built bit by bit as with the reference. */
+GBS_API int gbs_get_bit(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uint64_t col, int *value);
+GBS_API int gbs_set_bit(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uint64_t col, int value);
+
+/* BitSerialMatrix::clearAll (gemmbitserial.hpp:95-98): zeroes every plane of
+ * one side on `stream` (and marks the side imported). */
+GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);
 
 /* Forces the variant of a context's pipe: CUDA-core tile class (0: 64x64,
  * 1: 32x128, 2: 16x256 outputs per CTA), tensor-core N tile (128 or 256 rows

@@ -18,6 +18,7 @@
 
 #include <stdint.h>
 
+#include <cstdio>
 #include <stdexcept>
 #include <string>
 
@@ -33,10 +34,10 @@ template <typename T> struct elem;
 template <> struct elem<int8_t> { static const int code = GBS_I8; };
 template <> struct elem<int16_t> { static const int code = GBS_I16; };
 template <> struct elem<int32_t> { static const int code = GBS_I32; };
-// element types of importRegularAndQuantize<T>, which also takes uint8_t and float
+template <> struct elem<float> { static const int code = GBS_F32; };
+// element types of importRegularAndQuantize<T>, which also takes uint8_t
 template <typename T> struct qelem { static const int code = elem<T>::code; };
 template <> struct qelem<uint8_t> { static const int code = GBS_U8; };
-template <> struct qelem<float> { static const int code = GBS_F32; };
 }  // namespace detail
 
 class BitSerialMatrix {
@@ -83,7 +84,7 @@ class BitSerialMatrix {
   uint64_t wordsPerRow() const { return ncols_a / 64; }
   uint64_t wordsPerBitplane() const { return nrows_a * wordsPerRow(); }
 
-  // importRegular<T> (reference gemmbitserial.hpp:213): int8/int16/int32,
+  // importRegular<T> (reference gemmbitserial.hpp:213): int8/int16/int32/float,
   // host or device memory, row-major or (readColMajor) column-major.
   template <typename T>
   void importRegular(T *matrix, bool readColMajor = false) {
@@ -100,6 +101,62 @@ class BitSerialMatrix {
   void importRegularAndQuantize(T *matrix, T *thresholds, int nThres, bool readColMajor = false) {
     detail::check(gbs_import_quantize(ctx_, side_, matrix, thresholds, nThres, detail::qelem<T>::code,
                                       readColMajor ? 1 : 0, nullptr));
+  }
+
+  // Single bits (reference gemmbitserial.hpp:90-108, 126-129).  The planes
+  // live on the device: each call synchronises it and moves one word.
+  uint64_t bitpos(uint64_t col) const { return col & 63; }
+  bool get(uint64_t bit, uint64_t row, uint64_t col) const {
+    int v = 0;
+    detail::check(gbs_get_bit(ctx_, side_, bit, row, col, &v));
+    return v != 0;
+  }
+  void set(uint64_t bit, uint64_t row, uint64_t col) { detail::check(gbs_set_bit(ctx_, side_, bit, row, col, 1)); }
+  void unset(uint64_t bit, uint64_t row, uint64_t col) { detail::check(gbs_set_bit(ctx_, side_, bit, row, col, 0)); }
+  void clearAll() { detail::check(gbs_clear(ctx_, side_, nullptr)); }
+  // DEVICE pointers into the planes (reference :117-124)
+  uint64_t *rowptr(uint64_t bit, uint64_t row) { return data + bit * wordsPerBitplane() + row * wordsPerRow(); }
+  uint64_t *bitplaneptr(uint64_t bit) { return data + bit * wordsPerBitplane(); }
+
+  // quantize<T> (reference gemmbitserial.hpp:170-186): the code an element
+  // is stored as (float: casts truncate toward zero, then the low byte).
+  template <typename T>
+  uint8_t quantize(T x) const {
+    if (isBipolar()) return x > 0 ? 1 : 0;
+    if (issigned && x < 0) {
+      const int64_t h = (int64_t)1 << (nbits - 1);
+      return (uint8_t)(h + (int64_t)(x + h));  // x + h in int64 (integer T) or float, as the reference
+    }
+    return (uint8_t)(int64_t)x;
+  }
+  // importRegular_naive (reference :136-166): the same result as importRegular
+  template <typename T>
+  void importRegular_naive(T *matrix, bool readColMajor = false) {
+    importRegular(matrix, readColMajor);
+  }
+
+  void printSummary() const {
+    std::printf("BitSerialMatrix\nBits of precision: %llu signed: %d\nActual size: %llu x %llu\n"
+                "Allocated size: %llu x %llu\n",
+                (unsigned long long)nbits, (int)issigned, (unsigned long long)nrows, (unsigned long long)ncols,
+                (unsigned long long)nrows_a, (unsigned long long)ncols_a);
+  }
+  void printHex() const {
+    const uint64_t n = nbits * wordsPerBitplane();
+    uint64_t *w = new uint64_t[n ? n : 1];
+    int rc = gbs_get_planes(ctx_, side_, w, nullptr);
+    if (rc == GBS_OK)
+      for (uint64_t i = 0; i < nbits; i++) {
+        std::printf("Bit %llu:\n", (unsigned long long)i);
+        for (uint64_t j = 0; j < nrows_a; j++) {
+          for (uint64_t k = 0; k < wordsPerRow(); k++)
+            std::printf("%llx ", (unsigned long long)w[(i * nrows_a + j) * wordsPerRow() + k]);
+          std::printf("\n");
+        }
+        std::printf("\n");
+      }
+    delete[] w;
+    detail::check(rc);
   }
 
   // exportRegular<T> (reference gemmbitserial.hpp:313-333) into host memory.
@@ -122,6 +179,14 @@ class GEMMContext {
   uint64_t lhsBlock = 0, rhsBlock = 0;
   int32_t *res = nullptr;  // host, rhs.nrows x lhs.nrows (transposed result)
   gbs_ctx *handle = nullptr;
+
+  void printSummary() const {
+    std::printf("GEMMContext\nLHS: ");
+    lhs.printSummary();
+    std::printf("RHS: ");
+    rhs.printSummary();
+    std::printf("Block size: %llu x %llu\n", (unsigned long long)lhsBlock, (unsigned long long)rhsBlock);
+  }
 
   bool isBipolarTimesRegular() const { return lhs.isBipolar() != rhs.isBipolar(); }
   bool isBipolarTimesBipolar() const { return lhs.isBipolar() && rhs.isBipolar(); }

@@ -159,6 +159,20 @@ static int64_t load_elem(const void *src, int dtype, uint64_t idx) {
  * (raw bits, no quantisation).  For non-bipolar matrices both reduce to the
  * low bits of (uint8_t)x: the signed branch adds 2^(w-1) twice, i.e. 2^w,
  * which leaves the low w bits unchanged.  The bipolar branch maps x>0 to 1. */
+/* quantize<float> (gemmbitserial.hpp:170-186) for float input: bipolar maps
+ * x > 0 to 1; a negative x of a signed matrix becomes 2^(w-1) + (uint8_t)(x +
+ * 2^(w-1)) with the sum taken in float and truncated; otherwise (uint8_t)x.
+ * The float -> uint8_t casts are taken as truncation toward zero to an
+ * integer, then its low byte (C defines them only for values in [0, 256)). */
+static uint8_t to_code_f32(const orc_matrix *m, float x) {
+  if (mat_bipolar(m)) return x > 0 ? 1 : 0;
+  if (m->issigned && x < 0) {
+    const int64_t h = (int64_t)1 << (m->nbits - 1);
+    return (uint8_t)(h + (int64_t)(x + (float)h));
+  }
+  return (uint8_t)(int64_t)x;
+}
+
 static uint8_t to_code(const orc_matrix *m, int dtype, int64_t x) {
   if (dtype == ORC_U8) return (uint8_t)x;
   if (mat_bipolar(m)) return x > 0 ? 1 : 0;
@@ -177,7 +191,7 @@ static void mat_import(orc_matrix *m, const void *src, int dtype, int colmajor) 
   for (uint64_t r = 0; r < m->nrows; r++) {
     for (uint64_t col = 0; col < m->ncols; col++) {
       uint64_t idx = colmajor ? col * m->nrows + r : r * m->ncols + col;
-      uint8_t q = to_code(m, dtype, load_elem(src, dtype, idx));
+      uint8_t q = dtype == ORC_F32 ? to_code_f32(m, ((const float *)src)[idx]) : to_code(m, dtype, load_elem(src, dtype, idx));
       for (uint64_t b = 0; b < m->nbits; b++)
         if ((q >> b) & 1u) mat_row(m, b, r)[col >> 6] |= (uint64_t)1 << (col & 63);
     }

@@ -243,3 +243,24 @@ def ref_quantize_values(arr: np.ndarray, thresholds: np.ndarray, bits: int, colm
     ref().ref_quantize_export(rows, cols, bits, _ptr(arr), _ptr(thr) if thr.size else None, nthres,
                               _NP2DT[arr.dtype], int(colmajor), _ptr(out))
     return out
+
+
+def import_values(arr: np.ndarray, bits: int, signed: bool, colmajor: bool = False) -> np.ndarray:
+    """The values a ``bits``-bit matrix holds after importRegular of ``arr`` (exportRegular of it)."""
+    arr = np.ascontiguousarray(arr)
+    rows, cols = (arr.shape[1], arr.shape[0]) if colmajor else arr.shape
+    ctx = OracleContext(rows, cols, 1, bits, 1, signed, False)
+    ctx.import_(0, arr, colmajor)
+    out = np.zeros((rows, cols), np.int32)
+    if rows * cols:
+        lib().orc_export(ctx.h, 0, _ptr(out))
+    return out
+
+
+def ref_import_values(arr: np.ndarray, bits: int, signed: bool) -> np.ndarray:
+    """The same through the compiled reference (row-major input)."""
+    arr = np.ascontiguousarray(arr)
+    rows, cols = arr.shape
+    out = np.zeros((rows, cols), np.int32)
+    ref().ref_roundtrip(rows, cols, bits, int(bool(signed)), _ptr(arr), _NP2DT[arr.dtype], _ptr(out))
+    return out

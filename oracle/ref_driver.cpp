@@ -24,6 +24,7 @@ void do_import(BitSerialMatrix &m, const void *src, int dtype, bool colmajor) {
     case I8: m.importRegular((int8_t *)src, colmajor); break;
     case U8: m.importRegular((uint8_t *)src, colmajor); break;  // non-template overload
     case I16: m.importRegular((int16_t *)src, colmajor); break;
+    case F32: m.importRegular((float *)src, colmajor); break;
     default: m.importRegular((int32_t *)src, colmajor); break;
   }
 }

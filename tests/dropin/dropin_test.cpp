@@ -217,6 +217,44 @@ int main() {
       }
     failed += report("threshold-quantised import", ok, total);
   }
+  {  // float importRegular, quantize<T>, and matrices built bit by bit with set / get / unset / clearAll
+    int ok = 0, total = 0;
+    for (int d : {5, 64, 130}) {
+      const int M = d, K = d + 17, N = d / 2 + 1;
+      std::vector<float> af(M * K);
+      for (auto &x : af) x = (float)((int)(next_u64() % 800) - 400) / 100.f;  // [-4, 4)
+      GEMMContext ctx = allocGEMMContext(M, K, N, 3, 2, true, false);
+      ctx.lhs.importRegular(af.data());
+      std::vector<int8_t> qa(M * K);  // the codes the reference's quantize<float> produces, as values
+      for (int i = 0; i < M * K; i++) {
+        const uint8_t q = ctx.lhs.quantize(af[i]) & 7;
+        qa[i] = (int8_t)(q >= 4 ? q - 8 : q);
+      }
+      ctx.rhs.clearAll();
+      std::vector<int8_t> bt(N * K, 0);
+      for (int n = 0; n < N; n++)
+        for (int k = 0; k < K; k += 3) {
+          const int v = (int)(next_u64() % 4);
+          bt[n * K + k] = (int8_t)v;
+          if (v & 1) ctx.rhs.set(0, n, k);
+          if (v & 2) ctx.rhs.set(1, n, k);
+        }
+      ok += ctx.rhs.get(0, 0, 0) == ((bt[0] & 1) != 0);
+      total++;
+      ctx.rhs.set(1, N - 1, K - 1);
+      ctx.rhs.unset(1, N - 1, K - 1);
+      bt[(N - 1) * K + K - 1] &= 1;
+      if (ctx.rhs.get(0, N - 1, K - 1)) bt[(N - 1) * K + K - 1] |= 1;
+      std::vector<int32_t> want(M * N);
+      naive(qa, bt, want, M, K, N);
+      gemmBitSerial(ctx);
+      ok += memcmp(ctx.res, want.data(), M * N * 4) == 0;
+      total++;
+      if (d == 5) ctx.printSummary();
+      deallocGEMMContext(ctx);
+    }
+    failed += report("float import, quantize and single bits", ok, total);
+  }
   printf(failed ? "Some tests failed\n" : "All tests completed successfully\n");
   return failed;
 }

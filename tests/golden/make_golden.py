@@ -18,6 +18,8 @@ Writes
                      out-of-range values, odd shapes, K not a multiple of 64).
   ref_configs.json-- sha256 of the reference's int32 results on the full-size
                      benchmark workloads (seeded by gemmbitserial_gb300.datagen).
+  ref_float_import.npz -- importRegular<float> through the reference, then
+                     exportRegular, for every width and encoding.
   ref_quantize.npz -- importRegularAndQuantize (gemmbitserial.hpp:282-305) through
                      the reference, then exportRegular: inputs, thresholds
                      [nThres][rows] and the resulting values, for every element
@@ -186,6 +188,31 @@ def make_quantize() -> None:
     np.savez_compressed(os.path.join(HERE, "ref_quantize.npz"), **out)
 
 
+def make_float_import() -> None:
+    """importRegular<float> (quantize<float>, gemmbitserial.hpp:170-186) through the reference,
+    then exportRegular: values inside each encoding's defined range, fractions included."""
+    out = {}
+    i = 0
+    for bits in (1, 2, 3, 4, 8):
+        for sgn in (False, True):
+            for rows, cols in ((7, 70), (33, 129), (1, 5)):
+                rng = np.random.default_rng(5000 + i)
+                if sgn and bits > 1:
+                    lo, hi = -(1 << (bits - 1)), 1 << (bits - 1)
+                elif sgn:
+                    lo, hi = -3, 3
+                else:
+                    lo, hi = 0, min(256, 1 << bits)
+                a = rng.uniform(lo, hi - 1e-3, (rows, cols)).astype(np.float32)
+                a[0, :min(3, cols)] = [lo, 0.0, -0.0][:min(3, cols)]
+                key = f"f{i}"
+                out[key + "_src"] = a
+                out[key + "_meta"] = np.array([bits, int(sgn)], np.int64)
+                out[key + "_values"] = O.ref_import_values(a, bits, sgn)
+                i += 1
+    np.savez_compressed(os.path.join(HERE, "ref_float_import.npz"), **out)
+
+
 def make_config_hashes() -> None:
     res = {}
     for name in datagen.WORKLOADS:
@@ -205,5 +232,6 @@ if __name__ == "__main__":
     make_mnist(refdir)
     make_vectors()
     make_quantize()
+    make_float_import()
     make_config_hashes()
     print("golden fixtures written to", HERE)

@@ -212,8 +212,8 @@ def test_error_paths(lib):
     with pytest.raises(_capi.GBSError) as e:
         gemmBitSerial(ctx)  # no import yet
     assert e.value.code == _capi.GBS_ESTATE
-    with pytest.raises(TypeError):
-        ctx.lhs.importRegular(np.zeros((8, 64), np.float32))
+    with pytest.raises(TypeError):  # float32 is accepted (importRegular<float>); float64 is not
+        ctx.lhs.importRegular(np.zeros((8, 64), np.float64))
     deallocGEMMContext(ctx)
     # host-side allocation failure injection: reported, nothing leaks, library stays usable
     for n in (1, 2, 3, 4):

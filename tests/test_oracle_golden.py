@@ -151,3 +151,17 @@ def test_quantize_oracle_rejects_signed():
     ctx = O.OracleContext(4, 64, 4, 2, 2, True, False)
     with pytest.raises(ValueError):
         ctx.import_quantize(0, np.zeros((4, 64), np.int8), np.zeros((1, 4), np.int8))
+
+
+def test_float_import_oracle_matches_reference_fixtures():
+    """importRegular<float> (quantize<float>, gemmbitserial.hpp:170-186): the C restatement
+    against the reference's own results, fractional and negative values included."""
+    z = np.load(os.path.join(GOLD, "ref_float_import.npz"))
+    keys = sorted({k.rsplit("_", 1)[0] for k in z.files})
+    assert len(keys) >= 30
+    for k in keys:
+        bits, sgn = (int(x) for x in z[k + "_meta"])
+        got = O.import_values(z[k + "_src"], bits, bool(sgn))
+        assert np.array_equal(got, z[k + "_values"]), k
+        if O.ref_available():
+            assert np.array_equal(O.ref_import_values(z[k + "_src"], bits, bool(sgn)), z[k + "_values"]), k
