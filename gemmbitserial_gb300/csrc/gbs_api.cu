@@ -423,6 +423,12 @@ int gbs_import_quantize(gbs_ctx *c, int side, const void *src, const void *thres
   }
   e = launch_pack_quantize(m, dsrc, dthr, nthres, dtype, col_major ? 1 : 0, digits, dtab, s);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: pack kernel");
+  if (host && dsrc == c->stage[side]) {  // later host imports of this side wait before reusing the staging buffer
+    e = ensure_import_streams(c);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_packed[side], s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import_quantize: event record");
+    c->ev_packed_set[side] = true;
+  }
   if (digits) c->digits_valid[side] = true;
   m.imported = true;
   if (host) {  // host memory may be reused on return
