@@ -418,7 +418,8 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 //   warps 2-5  epilogue of this CTA's 128 rows
 // A cluster barrier closes the kernel, so no CTA frees TMEM or exits while
 // its peer may still signal its barriers or write its accumulator.
-constexpr int kPairStagesMax = 6;
+constexpr int kPairStagesMax = 7;
+constexpr size_t kPairSmemCap = 227 * 1024;  // the per-block dynamic shared memory limit
 constexpr int kPairThreads = 192;
 constexpr uint32_t kPairHalfBytes = 128 * kRowB;  // 128 rows x 128 digits
 
@@ -451,6 +452,38 @@ __device__ __forceinline__ void mma_commit_pair(uint32_t bar) {  // arrives on `
       "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
       "h"((uint16_t)3)
       : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+        "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+        "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+}
+// Waits for this thread's TMEM loads; the registers they fill are operands,
+// so no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                 "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]),
+                 "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]),
+                 "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]),
+                 "+r"(v[30]), "+r"(v[31])
+               :
+               : "memory");
+}
+// 32 columns n0 .. n0+31 of result row m: res[n*M + m], lanes on consecutive m.
+__device__ __forceinline__ void store_cols(const TmaArgs &a, const uint32_t (&v)[32], uint64_t gm, uint64_t n0) {
+  if (gm >= a.M) return;
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    const uint64_t gn = n0 + j;
+    if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
+  }
 }
 
 __global__ void __launch_bounds__(kPairThreads, 1)
@@ -547,26 +580,14 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       const int q = warp & 3;
       const uint64_t gm = m0 + q * 32 + lane;
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16);
+      // one 32-column TMEM load at a time (measured faster than keeping the
+      // next load in flight during the stores)
 #pragma unroll 1
       for (int col = 0; col < 256; col += 32) {
         uint32_t v[32];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-              "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-              "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-            : "r"(taddr + (uint32_t)col));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (gm < a.M) {
-#pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const uint64_t gn = n0 + col + j;
-            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
-          }
-        }
+        tmem_ld32(taddr + (uint32_t)col, v);
+        tmem_wait_ld(v);
+        store_cols(a, v, gm, n0 + col);
       }
     }
   }
@@ -859,13 +880,10 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   if (bn_req == kPairVariant || bn_req < 0) {  // 256 x 256 tiles on SM pairs
     a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
     const size_t stage_bytes = 2 * kPairHalfBytes;
-    // 16 KB of slack past the barriers: no operand read of the last stage can
-    // leave the allocation even if it spanned a whole 256-row tile
-    const size_t slack = kPairHalfBytes;
     int stages = kPairStagesMax;
-    while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 + slack > kSmemCap) stages--;
+    while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 > kPairSmemCap) stages--;
     a.stages = stages;
-    const size_t smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 + slack;
+    const size_t smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16;
     cudaError_t e = cudaFuncSetAttribute(gemm_tc_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg;
