@@ -289,6 +289,49 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2, mix=None, desc=None):
             "mix": desc or "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
 
 
+def measure_configs(lib, dev, stream, reps=50, warmup=5):
+    """Every named workload (C1, C2, C3a, C3b, the adjoint layer's forward): forward time with packed
+    operands resident and L2 flushed before each launch, the pipe the built-in rule chose, its rate,
+    bytes moved, and bit-exactness against the reference's own result (sha256)."""
+    import torch
+    from gemmbitserial_gb300 import _capi, datagen
+    from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", "ref_configs.json")))
+    names = {_capi.GBS_PIPE_POPC: "popc", _capi.GBS_PIPE_BMMA: "b1-mma", _capi.GBS_PIPE_TC: "tcgen05-digits",
+             _capi.GBS_PIPE_TC_PAIRS: "tcgen05-plane-pairs", _capi.GBS_PIPE_TC_SMEM: "tcgen05-smem-digits"}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    sh = C.c_void_p(stream.cuda_stream)
+    out = {}
+    for name in datagen.WORKLOADS:
+        M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+        ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+        with torch.cuda.stream(stream):
+            ctx.lhs.importRegular(torch.from_numpy(A).to(dev), stream=stream)
+            ctx.rhs.importRegular(torch.from_numpy(B).to(dev), stream=stream)
+            for _ in range(warmup):
+                flush.zero_()
+                _capi.check(lib.gbs_gemm(ctx._h, sh))
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for e0, e1 in ev:
+                flush.zero_()
+                e0.record(stream)
+                _capi.check(lib.gbs_gemm(ctx._h, sh))
+                e1.record(stream)
+        stream.synchronize()
+        ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+        res = ctx.res.reshape(N, M)
+        ok = hashlib.sha256(np.ascontiguousarray(res).tobytes()).hexdigest() == gold.get(name, {}).get("sha256")
+        pipe = ctx.pipe
+        deallocGEMMContext(ctx)
+        kpad = (K + 63) // 64 * 64
+        packed = wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N
+        out[name] = {"ms": round(ms, 4), "gops": round(gops(M, K, N, ms * 1e-3), 1), "pipe": names.get(pipe, pipe),
+                     "tbinops": round(2.0 * M * N * kpad * wA * wB / (ms * 1e-3) / 1e12, 2),
+                     "gbs_packed_bytes": round(packed / (ms * 1e-3) / 1e9, 1),
+                     "parity": "bit-exact vs reference (sha256)" if ok else "MISMATCH"}
+    return out
+
+
 def measure_adjoint(lib, dev, stream, reps=10, warmup=3):
     """QAT layer adjoint: A 4096x2048 u2, B 2048x2048 bipolar, dC ~ N(0,1).  Ours (FP32 from the packed
     planes) vs the plain GPU path (export values, two FP32 cuBLAS matmuls with TF32 off)."""
@@ -504,6 +547,7 @@ def run_ours(args):
     roof["algorithmic_bytes"] = int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)
     clocks = clk.summary()
 
+    configs = measure_configs(lib, dev, stream)
     grouped = None if args.no_grouped else measure_grouped(lib, dev, stream)
     caffenet = None
     if not args.no_grouped:  # the reference's CaffeNet chain (benchmark.cpp:174-237) as a second group
@@ -529,7 +573,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),
                     "ms_per_step": round(e2e_s * 1e3, 4), "parity": "bit-exact" if e2e_ok else "MISMATCH"},
             "roofline": roof,
-            "grouped": grouped, "caffenet": caffenet, "adjoint": adjoint,
+            "configs": configs, "grouped": grouped, "caffenet": caffenet, "adjoint": adjoint,
             "cpu_baseline": cpu, "gpu_launches": int(launches), "clocks": clocks,
             "wall_s_timed_region": round(t_wall, 4)}
     print(json.dumps(line), flush=True)
