@@ -50,13 +50,6 @@ __device__ __forceinline__ uint32_t elem_code(const void *src, int dtype, uint64
   return code_of(load_elem(src, dtype, idx), dtype, bipolar);
 }
 
-// Bits b of the four bytes of x, gathered into a nibble (byte i -> bit i).
-// (x>>b)&0x01010101 leaves one bit per byte at positions 0, 8, 16, 24; the
-// multiply by 1 + 2^7 + 2^14 + 2^21 lands them, carry-free, at 21..24.
-__device__ __forceinline__ uint32_t nibble(uint32_t x, int b) {
-  return ((((x >> b) & 0x01010101u) * 0x00204081u) >> 21) & 0xfu;
-}
-
 // Row-major packing: a warp takes a 1024-column segment of one padded row;
 // lane l owns the 32 columns [seg*1024 + 32l, +32).  Its 32 codes (byte j%4
 // of q[j/4]) give, per plane, one whole 32-bit half of a plane word, so the
@@ -85,10 +78,19 @@ __device__ __forceinline__ void load_codes32(const void *__restrict__ src, int d
       for (int i = 0; i < 8; i++) q[i] = __vcmpgts4(q[i], 0u) & 0x01010101u;
     }
   } else {
-#pragma unroll 4
+#pragma unroll
     for (int j = 0; j < 32; j++)
       if (col0 + j < ncols) q[j >> 2] |= elem_code(src, dtype, base + j, bipolar, issigned, nbits) << (8 * (j & 3));
   }
+}
+
+// Bits b of the eight bytes of (hi:lo), gathered into a byte (byte i -> bit i):
+// masking leaves one bit per byte at 8i; the multiply by sum_i 2^(56-7i)
+// moves it to 56+i.  All partial products land on distinct bit positions
+// (8i - 7j is unique for i, j in 0..7), so nothing carries.
+__device__ __forceinline__ uint32_t gather8(uint32_t lo, uint32_t hi, int b) {
+  const uint64_t x = ((((uint64_t)hi << 32) | lo) >> b) & 0x0101010101010101ull;
+  return (uint32_t)((x * 0x0102040810204080ull) >> 56);
 }
 
 __device__ __forceinline__ void emit_planes32(int nbits, uint64_t nrows_a, uint64_t wpr, uint64_t *__restrict__ planes,
@@ -96,9 +98,8 @@ __device__ __forceinline__ void emit_planes32(int nbits, uint64_t nrows_a, uint6
   uint32_t *p32 = reinterpret_cast<uint32_t *>(planes);  // little-endian halves of the u64 plane words
   const uint64_t row32 = 2 * wpr, idx = r * row32 + (col0 >> 5), plane32 = nrows_a * row32;
   for (int b = 0; b < nbits; b++) {
-    uint32_t w = 0u;
-#pragma unroll
-    for (int i = 0; i < 8; i++) w |= nibble(q[i], b) << (4 * i);
+    const uint32_t w = gather8(q[0], q[1], b) | (gather8(q[2], q[3], b) << 8) | (gather8(q[4], q[5], b) << 16) |
+                       (gather8(q[6], q[7], b) << 24);
     p32[b * plane32 + idx] = w;
   }
 }
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(256) pack_quantize_kernel(const T *__restrict_
 #pragma unroll
   for (int i = 0; i < 8; i++) q[i] = 0u;
   if (r < nrows) {
-#pragma unroll 4
+#pragma unroll
     for (int j = 0; j < 32; j++) {
       const uint64_t c = col0 + j;
       if (c < ncols) {
@@ -256,14 +257,11 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
   for (uint64_t base = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRun; base < total;
        base += nw * kRun) {
     int j = find_job(jobs, njobs, base);
-#pragma unroll 1
-    for (int u = 0; u < kRun; u++) {
-      const uint64_t w = base + u;
-      if (w >= total) break;
-      while (j + 1 < njobs && jobs[j + 1].warp0 <= w) j++;
-      const PackJob &J = jobs[j];
+    // unit w -> (job, row, segment), advancing the job index monotonically
+    auto locate = [&](uint64_t w, int &jj, uint64_t &r, uint64_t &sg) {
+      while (jj + 1 < njobs && jobs[jj + 1].warp0 <= w) jj++;
+      const PackJob &J = jobs[jj];
       const uint64_t local = w - J.warp0;
-      uint64_t r, sg;
       if (local < 0xFFFFFFFFull) {  // 32-bit division in the common case
         const uint32_t l32 = (uint32_t)local, r32 = l32 / J.segs;
         r = r32;
@@ -272,10 +270,46 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
         r = local / J.segs;
         sg = local % J.segs;
       }
-      const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
-      pack_unit(J.src, J.dtype, J.nbits == 1 && J.issigned, J.issigned, J.nbits, J.nrows, J.ncols, J.nrows_a, J.wpr,
-                J.vec,
-                J.planes, J.digits, tab, r, sg, lane);
+    };
+    auto load = [&](int jj, uint64_t r, uint64_t sg, uint32_t (&q)[8]) {
+      const PackJob &J = jobs[jj];
+      const uint64_t col0 = sg * kSegCols + (uint64_t)lane * 32;
+      if (col0 < J.wpr * 64)
+        load_codes32(J.src, J.dtype, J.nbits == 1 && J.issigned, J.issigned, J.nbits, J.nrows, J.ncols, J.vec, r,
+                     col0, q);
+    };
+    // the next unit's loads are in flight while the current unit is packed
+    const uint64_t last = min(base + (uint64_t)kRun, total);
+    int jc = j;
+    uint64_t rc, sc;
+    locate(base, jc, rc, sc);
+    uint32_t q[8];
+    load(jc, rc, sc, q);
+#pragma unroll 1
+    for (uint64_t w = base; w < last; w++) {
+      int jn = jc;
+      uint64_t rn = 0, sn = 0;
+      uint32_t qn[8];
+      if (w + 1 < last) {
+        locate(w + 1, jn, rn, sn);
+        load(jn, rn, sn, qn);
+      }
+      const PackJob &J = jobs[jc];
+      const uint64_t col0 = sc * kSegCols + (uint64_t)lane * 32;
+      if (col0 < J.wpr * 64) {
+        emit_planes32(J.nbits, J.nrows_a, J.wpr, J.planes, rc, col0, q);
+        if (J.digits) {
+          const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
+          write_digits32(J.digits, J.nbits, J.nrows, J.ncols, J.wpr, tab, rc, col0, q);
+        }
+      }
+      if (w + 1 < last) {
+        jc = jn;
+        rc = rn;
+        sc = sn;
+#pragma unroll
+        for (int i = 0; i < 8; i++) q[i] = qn[i];
+      }
     }
   }
 }
@@ -301,11 +335,13 @@ __global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ sr
     const uint64_t c = w * 64 + half * 32 + lane;
     uint32_t q[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};  // codes of rows r0..r0+31 of column c
     if (c < ncols) {
+#pragma unroll
       for (int j = 0; j < 32; j++) {
         uint64_t r = r0 + j;
         if (r < nrows) q[j >> 2] |= elem_code(src, dtype, c * nrows + r, bipolar, issigned, nbits) << (8 * (j & 3));
       }
     }
+#pragma unroll
     for (int j = 0; j < 32; j++) {
       uint32_t code = (q[j >> 2] >> (8 * (j & 3))) & 0xffu;
 #pragma unroll
