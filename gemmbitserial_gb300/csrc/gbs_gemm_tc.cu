@@ -293,6 +293,7 @@ struct TmaArgs {
   uint32_t nstages;
   uint32_t idesc;
   int stages;
+  int splits;  // SM-pair kernel: K chunks per output tile, one SM pair each (1, 2 or 4)
 };
 
 template <int BN>
@@ -447,11 +448,20 @@ __device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint6
       " tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
 }
-__device__ __forceinline__ void mma_commit_pair(uint32_t bar) {  // arrives on `bar` in both CTAs
+// arrives on `bar` in both CTAs of the pair whose ranks are the set bits of `mask`
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t mask) {
   asm volatile(
       "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
-      "h"((uint16_t)3)
+      "h"(mask)
       : "memory");
+}
+// Generic address of the same shared-memory location in CTA `rank` of the
+// cluster: plain loads through it can be batched by the compiler.
+template <typename T>
+__device__ __forceinline__ const T *cluster_ptr(const T *p, uint32_t rank) {
+  uint64_t d;
+  asm("mapa.u64 %0, %1, %2;" : "=l"(d) : "l"(reinterpret_cast<uint64_t>(p)), "r"(rank));
+  return reinterpret_cast<const T *>(d);
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
@@ -486,20 +496,27 @@ __device__ __forceinline__ void store_cols(const TmaArgs &a, const uint32_t (&v)
   }
 }
 
+template <int SPLITS>
 __global__ void __launch_bounds__(kPairThreads, 1)
     gemm_tc_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TmaArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t rank = cluster_rank();
+  // ranks 2p and 2p+1 form the SM pair of K chunk p; the even one leads
+  const uint32_t peer = rank & 1u, split = rank >> 1, lead = rank & ~1u;
+  const uint16_t pair_mask = (uint16_t)(3u << lead);
   const uint32_t stage_bytes = 2 * kPairHalfBytes;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.stages * stage_bytes);
   const uint32_t full = smem_u32(bars), empty = full + 8 * a.stages, acc_full = empty + 8 * a.stages;
   const uint32_t mma_done = acc_full + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * a.stages + 2);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-  const uint64_t pair_m0 = (uint64_t)(blockIdx.x >> 1) * 256, n0 = (uint64_t)blockIdx.y * 256;
-  const uint64_t m0 = pair_m0 + 128 * rank;
+  const uint64_t pair_m0 = (uint64_t)(blockIdx.x / (2 * SPLITS)) * 256, n0 = (uint64_t)blockIdx.y * 256;
+  const uint64_t m0 = pair_m0 + 128 * peer;
+  const uint32_t k_lo = split * a.nstages / SPLITS, k_hi = (split + 1) * a.nstages / SPLITS;
+  const uint32_t nk = k_hi - k_lo;
+  bool tile_done = false;  // epilogue warps: the accumulator is complete
 
   if (tid == 0) {
     for (int i = 0; i < a.stages; i++) {
@@ -526,14 +543,14 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       uint32_t issued = 0;
-      for (uint32_t k = 0; k < a.nstages; k++) {
+      for (uint32_t k = 0; k < nk; k++) {
         const uint32_t s = k % a.stages, use = k / a.stages;
         if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) break;
-        const uint32_t fb = map_to_rank(full + 8 * s, 0);
-        if (rank == 0) mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
+        const uint32_t fb = map_to_rank(full + 8 * s, lead);
+        if (peer == 0) mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
         const uint32_t dst = smem_u32(smem + s * stage_bytes);
-        tma_load_2d_pair(dst, &tmA, (int)(k * 128), (int)m0, fb);
-        tma_load_2d_pair(dst + kPairHalfBytes, &tmB, (int)(k * 128), (int)(n0 + 128 * rank), fb);
+        tma_load_2d_pair(dst, &tmA, (int)((k_lo + k) * 128), (int)m0, fb);
+        tma_load_2d_pair(dst + kPairHalfBytes, &tmB, (int)((k_lo + k) * 128), (int)(n0 + 128 * peer), fb);
         issued = k + 1;
       }
       // After an abort the leader waits (bounded) for the loads its barriers
@@ -541,7 +558,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       // peer cannot wait on, so a stopped peer sleeps ~0.2 ms instead: far
       // longer than a 16 KB load takes to land in its shared memory.
       if (*abort_flag) {
-        if (rank == 0) {
+        if (peer == 0) {
           for (uint32_t k = (issued > (uint32_t)a.stages ? issued - a.stages : 0); k < issued; k++)
             mbar_drain(full + 8 * (k % a.stages), (k / a.stages) & 1);
         } else {
@@ -550,9 +567,9 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       }
     }
   } else if (warp == 1) {
-    if (lane == 0 && rank == 0) {
+    if (lane == 0 && peer == 0) {
       bool ok = true;
-      for (uint32_t k = 0; k < a.nstages && ok; k++) {
+      for (uint32_t k = 0; k < nk && ok; k++) {
         const uint32_t s = k % a.stages;
         if (!mbar_wait(full + 8 * s, (k / a.stages) & 1, abort_flag)) {
           ok = false;
@@ -564,10 +581,10 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         for (int kk = 0; kk < 4; kk++)
           mma_f8_pair(tmem, sw128_desc(base + kk * 32), sw128_desc(base + kPairHalfBytes + kk * 32), a.idesc,
                       (k | kk) != 0);
-        mma_commit_pair(empty + 8 * s);
+        mma_commit_pair(empty + 8 * s, pair_mask);
       }
       if (ok) {
-        mma_commit_pair(acc_full);
+        mma_commit_pair(acc_full, pair_mask);
       } else {  // issued MMAs finish before TMEM is freed
         asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done)
                      : "memory");
@@ -575,25 +592,90 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       }
     }
   } else {
-    if (__all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag))) {
+    tile_done = __all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag));
+    if (tile_done) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int q = warp & 3;
       const uint64_t gm = m0 + q * 32 + lane;
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16);
-      // one 32-column TMEM load at a time (measured faster than keeping the
-      // next load in flight during the stores)
+      if (SPLITS == 1) {
+        // one 32-column TMEM load at a time (measured faster than keeping the
+        // next load in flight during the stores)
 #pragma unroll 1
-      for (int col = 0; col < 256; col += 32) {
-        uint32_t v[32];
-        tmem_ld32(taddr + (uint32_t)col, v);
-        tmem_wait_ld(v);
-        store_cols(a, v, gm, n0 + col);
+        for (int col = 0; col < 256; col += 32) {
+          uint32_t v[32];
+          tmem_ld32(taddr + (uint32_t)col, v);
+          tmem_wait_ld(v);
+          store_cols(a, v, gm, n0 + col);
+        }
+      } else {
+        // the columns the other K chunks reduce go into the drained ring as
+        // [64 column quads][128 rows][4 columns] fp32: each lane (row) writes,
+        // and later reads remotely, 16 bytes per quad, a warp 512 contiguous
+        // bytes; this chunk's own columns stay in TMEM
+        float4 *part = reinterpret_cast<float4 *>(smem) + q * 32 + lane;
+        const uint32_t own0 = split * (256u / SPLITS), own1 = own0 + 256u / SPLITS;
+#pragma unroll 1
+        for (uint32_t col = 0; col < 256; col += 32) {
+          if (col >= own0 && col < own1) continue;
+          uint32_t v[32];
+          tmem_ld32(taddr + (uint32_t)col, v);
+          tmem_wait_ld(v);
+#pragma unroll
+          for (int j = 0; j < 32; j += 4)
+            part[((col + j) >> 2) * 128] = make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]),
+                                                       __uint_as_float(v[j + 2]), __uint_as_float(v[j + 3]));
+        }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  if constexpr (SPLITS > 1) {
+    // Split-K reduction over distributed shared memory: the CTA of chunk p sums
+    // columns [p*256/S, (p+1)*256/S) of its 128 rows over the S partial tiles
+    // (integers below 2^24: the fp32 sums are exact) and stores them; a warp's
+    // remote loads and its stores each cover 32 consecutive rows of a column.
+    if (warp >= 2 && tile_done) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int q = warp & 3;
+      const uint32_t row = (uint32_t)(q * 32 + lane), cols = 256u / SPLITS, c0 = split * cols;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + c0;
+      const uint64_t gm = m0 + row;
+      const float4 *mine = reinterpret_cast<const float4 *>(smem) + (c0 >> 2) * 128 + row;
+      const float4 *src[SPLITS - 1];
+#pragma unroll
+      for (int qq = 1; qq < SPLITS; qq++) src[qq - 1] = cluster_ptr(mine, 2 * ((split + qq) % SPLITS) + peer);
+      // 32 columns at a time: the other chunks' partials (remote loads issued
+      // first), then this chunk's own from TMEM
+#pragma unroll 1
+      for (uint32_t cb = 0; cb < cols; cb += 32) {
+        float4 raw[SPLITS - 1][8];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+          for (int qq = 0; qq < SPLITS - 1; qq++) raw[qq][i] = src[qq][((cb >> 2) + i) * 128];
+        uint32_t v[32];
+        tmem_ld32(taddr + cb, v);
+        tmem_wait_ld(v);
+        if (gm < a.M) {
+#pragma unroll
+          for (int i = 0; i < 32; i++) {
+            float acc = __uint_as_float(v[i]);
+#pragma unroll
+            for (int qq = 0; qq < SPLITS - 1; qq++) {
+              const float4 r4 = raw[qq][i >> 2];
+              acc += (i & 3) == 0 ? r4.x : (i & 3) == 1 ? r4.y : (i & 3) == 2 ? r4.z : r4.w;
+            }
+            const uint64_t gn = n0 + c0 + cb + i;
+            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(acc);
+          }
+        }
+      }
+    }
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  }
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;");
     asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(256));
@@ -846,6 +928,64 @@ cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
 
 }  // namespace
 
+namespace {
+
+size_t pair_smem_bytes() {
+  const size_t stage_bytes = 2 * kPairHalfBytes;
+  int stages = kPairStagesMax;
+  while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 > kPairSmemCap) stages--;
+  return 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16;
+}
+
+template <int S>
+void pair_set_attrs(size_t smem) {
+  cudaFuncSetAttribute(gemm_tc_pair_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1], int splits, size_t smem,
+                        cudaStream_t s) {
+  if (splits == 4) pair_set_attrs<4>(smem);
+  else if (splits == 2) pair_set_attrs<2>(smem);
+  else pair_set_attrs<1>(smem);
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.blockDim = dim3(kPairThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2 * splits;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+}
+
+// Clusters of 2 * splits CTAs that fit the GPU at once (they are placed within
+// one GPC each), cached per device.
+int pair_max_clusters(int splits) {
+  static int cache[64][5] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  int &v = cache[dev][splits];
+  if (v == 0) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    pair_launch_config(cfg, attr, splits, pair_smem_bytes(), nullptr);
+    cfg.gridDim = dim3(2 * splits, 1, 1);
+    int n = 0;
+    cudaError_t e;
+    if (splits == 4) e = cudaOccupancyMaxActiveClusters(&n, gemm_tc_pair_kernel<4>, &cfg);
+    else e = cudaOccupancyMaxActiveClusters(&n, gemm_tc_pair_kernel<2>, &cfg);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      n = 0;
+    }
+    v = n > 0 ? n : -1;
+  }
+  return v > 0 ? v : 0;
+}
+
+}  // namespace
+
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   for (int side = 0; side < 2; side++)
     if (!c->digits_valid[side]) {
@@ -879,28 +1019,31 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   }
   if (bn_req == kPairVariant || bn_req < 0) {  // 256 x 256 tiles on SM pairs
     a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+    // Split K over up to 4 SM pairs per tile (a cluster of up to 8 CTAs) while
+    // the grid still fits one wave and every chunk keeps >= 8 stages: shapes
+    // with few output tiles and a long K then use the whole GPU.
+    const uint64_t pair_tiles = ((a.M + 255) / 256) * ((a.N + 255) / 256);
+    a.splits = 1;
+    for (int cand : {4, 2})
+      if (a.nstages / cand >= 8 && pair_tiles <= (uint64_t)pair_max_clusters(cand)) {
+        a.splits = cand;
+        break;
+      }
     const size_t stage_bytes = 2 * kPairHalfBytes;
     int stages = kPairStagesMax;
     while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 > kPairSmemCap) stages--;
     a.stages = stages;
     const size_t smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16;
-    cudaError_t e = cudaFuncSetAttribute(gemm_tc_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg;
-    memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3((unsigned)(2 * ((a.M + 255) / 256)), (unsigned)((a.N + 255) / 256));
-    cfg.blockDim = dim3(kPairThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel, *reinterpret_cast<const CUtensorMap *>(c->tc_map_da),
-                           *reinterpret_cast<const CUtensorMap *>(c->tc_map_db), a);
+    pair_launch_config(cfg, attr, a.splits, smem, s);
+    cfg.gridDim = dim3((unsigned)(2 * a.splits * ((a.M + 255) / 256)), (unsigned)((a.N + 255) / 256));
+    const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
+    const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_db);
+    cudaError_t e;
+    if (a.splits == 4) e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel<4>, ma, mb, a);
+    else if (a.splits == 2) e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel<2>, ma, mb, a);
+    else e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel<1>, ma, mb, a);
     count_launch();
     return e != cudaSuccess ? e : cudaGetLastError();
   }
