@@ -10,9 +10,11 @@ metric is the reference's GOPS = 2*M*K*N / time (benchmark/benchmark.cpp:107).
   with CUDA events on the launching stream; L2 is flushed (256 MiB write,
   outside the events) before every step.
 * e2e: the same metric through the C ABI from pinned HOST buffers: both
-  imports (host->device copy + pack), the GEMM and the result read-back.
-* roofline: the forward kernel's AND+popcount rate against the CUDA-core POPC
-  pipe's measured peak (gbs_pipe_peaks, run in this process).
+  imports (the pack kernels read the host buffers over the host link) and
+  gbs_gemm_to, whose kernels write the result into the host buffer -- the
+  calls the C++ drop-in's importRegular / gemmBitSerial make.
+* roofline: the forward kernel's rate against the measured peak of the pipe it
+  ran on (tcgen05 e4m3 for the default workload, measured in this process).
 * cpu_baseline: the reference's algorithm on this host's cores (the compiled
   reference when present, else the oracle's C restatement), same workload.
 
@@ -494,8 +496,8 @@ def run_ours(args):
     def e2e_step():
         _capi.check(lib.gbs_import(ctx2._h, 0, C.c_void_p(hA.data_ptr()), _capi.GBS_I8, 0, sh))
         _capi.check(lib.gbs_import(ctx2._h, 1, C.c_void_p(hB.data_ptr()), _capi.GBS_I8, 0, sh))
-        _capi.check(lib.gbs_gemm(ctx2._h, sh))
-        _capi.check(lib.gbs_get_result(ctx2._h, C.c_void_p(hR.data_ptr()), sh))
+        # gemmBitSerial + the read of ctx.res, as the C++ drop-in issues them
+        _capi.check(lib.gbs_gemm_to(ctx2._h, C.c_void_p(hR.data_ptr()), sh))
 
     for _ in range(args.warmup):
         e2e_step()

@@ -40,6 +40,7 @@ SIGNATURES = {
     "gbs_set_bit": (i32, [vp, i32, u64, u64, u64, i32]),
     "gbs_clear": (i32, [vp, i32, vp]),
     "gbs_gemm": (i32, [vp, vp]),
+    "gbs_gemm_to": (i32, [vp, vp, vp]),
     "gbs_get_result": (i32, [vp, vp, vp]),
     "gbs_sum_rows": (i32, [vp, i32, vp, vp]),
     "gbs_export": (i32, [vp, i32, vp, vp]),

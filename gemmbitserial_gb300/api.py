@@ -224,9 +224,29 @@ def allocGEMMContext(lhsRows, depth, rhsRows, lhsBits, rhsBits, lhsSigned, rhsSi
 allocateGEMMContext = allocGEMMContext  # the name README.md:15 uses
 
 
-def gemmBitSerial(ctx: GEMMContext, stream=None) -> None:
-    """gemmBitSerial (arch-generic.hpp:331-345); asynchronous on the stream."""
-    _capi.check(_capi.load().gbs_gemm(ctx._h, _stream_handle(stream)))
+def gemmBitSerial(ctx: GEMMContext, stream=None, out=None) -> None:
+    """gemmBitSerial (arch-generic.hpp:331-345); asynchronous on the stream.
+
+    With `out` (a C-contiguous int32 numpy array or torch tensor of N*M
+    elements, host or device), the result goes straight there (gbs_gemm_to)
+    and the call returns once it has landed when `out` is in host memory;
+    ctx.res is then stale until the next plain call."""
+    lib = _capi.load()
+    if out is None:
+        _capi.check(lib.gbs_gemm(ctx._h, _stream_handle(stream)))
+        return
+    info = ctx._info()
+    n = info.lhs.nrows * info.rhs.nrows
+    if hasattr(out, "data_ptr"):
+        import torch
+        if out.dtype != torch.int32 or not out.is_contiguous() or out.numel() < n:
+            raise ValueError("out must be a contiguous int32 tensor of at least N*M elements")
+        ptr = out.data_ptr()
+    else:
+        if out.dtype != np.int32 or not out.flags["C_CONTIGUOUS"] or out.size < n:
+            raise ValueError("out must be a C-contiguous int32 array of at least N*M elements")
+        ptr = out.ctypes.data
+    _capi.check(lib.gbs_gemm_to(ctx._h, C.c_void_p(ptr), _stream_handle(stream)))
 
 
 def deallocGEMMContext(ctx: GEMMContext) -> None:

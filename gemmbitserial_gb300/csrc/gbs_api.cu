@@ -73,6 +73,36 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Address through which this device reads or writes caller memory `p`, or
+// nullptr when it cannot: device and managed memory as they are, pinned host
+// memory through its mapped device address, and (with `pageable`) pageable
+// host memory as it is where the GPU walks the host's page tables
+// (NVLink-C2C systems such as GB300).  GBS_HOST_DIRECT=0 turns the host cases
+// off (staged copies instead).
+void *device_view(const void *p, int dev, bool pageable_ok) {
+  const char *env = getenv("GBS_HOST_DIRECT");
+  const bool host_direct = !(env && env[0] == '0');
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void *>(p);
+  if (!host_direct) return nullptr;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  static int pageable[64];  // 0 unknown, 1 yes, 2 no
+  if (!pageable_ok || dev < 0 || dev >= 64) return nullptr;
+  if (!pageable[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    pageable[dev] = v ? 1 : 2;
+  }
+  return pageable[dev] == 1 ? const_cast<void *>(p) : nullptr;
+}
+
 size_t elem_size(int dtype) { return dtype == GBS_I16 ? 2 : (dtype == GBS_I32 || dtype == GBS_F32) ? 4 : 1; }
 
 void free_ctx_buffers(gbs_ctx *c) {
@@ -305,7 +335,21 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
     }
   }
   cudaError_t e = cudaSuccess;
-  if (n && !is_device_ptr(src)) {
+  const void *view = (n && !is_device_ptr(src)) ? device_view(src, c->device, true) : nullptr;
+  if (view) {  // host memory the device reads directly: the pack kernel is the copy
+    if (!col_major) {
+      e = launch_pack_rows(m, view, dtype, 0, m.nrows_a, digits, dtab, s);
+      if (e == cudaSuccess && digits) c->digits_valid[side] = true;
+    } else {
+      e = launch_pack(m, view, dtype, 1, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack kernel");
+    e = ensure_import_streams(c);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_packed[side], s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(c->ev_packed[side]);  // host memory may be reused once read
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_import: pack wait");
+    c->ev_packed_set[side] = true;
+  } else if (n && !is_device_ptr(src)) {
     const size_t esz = elem_size(dtype), bytes = n * esz;
     int rc = ensure_stage(c, side, bytes, s);
     if (rc != GBS_OK) return rc;
@@ -543,7 +587,7 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   GemmShape sh;
   sh.A = c->lhs.planes;
   sh.B = c->rhs.planes;
-  sh.C = c->res;
+  sh.C = result_ptr(c);
   sh.M = M;
   sh.N = N;
   sh.wpr = c->lhs.wpr();
@@ -577,6 +621,37 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
     ke = launch_gemm_popc(sh, e, s);
   }
   if (ke != cudaSuccess) return cuda_fail(ke, "gbs_gemm: forward kernel");
+  if (!c->out) c->res_stale = false;
+  return GBS_OK;
+}
+
+int gbs_gemm_to(gbs_ctx *c, int32_t *dst, void *stream) {
+  if (!c) return fail(GBS_EINVAL, "gbs_gemm_to: ctx is NULL");
+  const uint64_t n = c->lhs.nrows * c->rhs.nrows;
+  if (n == 0) return gbs_gemm(c, stream);
+  if (!dst) return fail(GBS_EINVAL, "gbs_gemm_to: dst is NULL");
+  DeviceGuard g(c->device);
+  if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_gemm_to: cudaSetDevice");
+  cudaStream_t s = as_stream(stream);
+  const bool host = !is_device_ptr(dst);
+  // The epilogues store 16-byte vectors where rows allow: direct writes need an
+  // aligned buffer.  Pageable destinations take the copy: the copy engine
+  // writes them faster than the kernels' stores through the host page tables.
+  int32_t *view =
+      ((uintptr_t)dst % 16 == 0) ? static_cast<int32_t *>(device_view(dst, c->device, false)) : nullptr;
+  if (!view) {  // the device cannot write dst: compute into res, then copy
+    int rc = gbs_gemm(c, stream);
+    return rc != GBS_OK ? rc : gbs_get_result(c, dst, stream);
+  }
+  c->out = view;
+  const int rc = gbs_gemm(c, stream);
+  c->out = nullptr;
+  if (rc != GBS_OK) return rc;
+  c->res_stale = true;
+  if (host) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "gbs_gemm_to: stream sync");
+  }
   return GBS_OK;
 }
 
@@ -585,6 +660,8 @@ int gbs_get_result(gbs_ctx *c, int32_t *dst, void *stream) {
   const uint64_t n = c->lhs.nrows * c->rhs.nrows;
   if (n == 0) return GBS_OK;
   if (!dst) return fail(GBS_EINVAL, "gbs_get_result: dst is NULL");
+  if (c->res_stale)
+    return fail(GBS_ESTATE, "gbs_get_result: the last GEMM wrote its result to the caller's buffer (gbs_gemm_to)");
   DeviceGuard g(c->device);
   cudaStream_t s = as_stream(stream);
   cudaError_t e = cudaMemcpyAsync(dst, c->res, n * 4, cudaMemcpyDefault, s);

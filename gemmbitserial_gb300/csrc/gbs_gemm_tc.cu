@@ -866,7 +866,7 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn_req) 
   const Mat &A = c->lhs, &B = c->rhs;
   TcArgs a;
   memset(&a, 0, sizeof(a));
-  a.C = c->res;
+  a.C = result_ptr(c);
   a.M = A.nrows;
   a.N = B.nrows;
   a.K = A.ncols;
@@ -1000,7 +1000,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   }
   TmaArgs a;
   memset(&a, 0, sizeof(a));
-  a.C = c->res;
+  a.C = result_ptr(c);
   a.M = c->lhs.nrows;
   a.N = c->rhs.nrows;
   a.nstages = (uint32_t)(c->lhs.ncols_a / 128);
@@ -1015,7 +1015,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     }
     uint32_t *err = tc_error_ptr();
     if (!err) return cudaErrorInvalidSymbol;
-    return tcg_gemm(*c->plan1, err, s);
+    return tcg_gemm(*c->plan1, err, s, c->out);
   }
   if (bn_req == kPairVariant || bn_req < 0) {  // 256 x 256 tiles on SM pairs
     a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);

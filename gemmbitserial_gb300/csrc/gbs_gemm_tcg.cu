@@ -59,7 +59,8 @@ __device__ __forceinline__ bool tile_ok(const TcgTile &t, const TcgProblem &P, u
 
 __global__ void __launch_bounds__(kTgThreads, 1)
     gemm_tcg_kernel(const TcgProblem *__restrict__ probs, const CUtensorMap *__restrict__ maps,
-                    const TcgTile *__restrict__ tiles, uint32_t ntiles, uint32_t nprob, uint32_t *err) {
+                    const TcgTile *__restrict__ tiles, uint32_t ntiles, uint32_t nprob, uint32_t *err,
+                    int32_t *out0) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -178,6 +179,7 @@ __global__ void __launch_bounds__(kTgThreads, 1)
         if (warp == 2 && lane == 0) atomicOr(err, 4u);
         continue;
       }
+      if (out0 && tl.p == 0) P.C = out0;  // the caller's result buffer for problem 0
       const uint32_t a = jt & 1, use = jt >> 1;
       if (!__all_sync(0xffffffffu, mbar_wait_err(acc_full + 8 * a, use & 1, abort_flag, err))) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
@@ -459,10 +461,11 @@ cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s) {
   return cudaSuccess;
 }
 
-cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s) {
+cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s, int32_t *out0) {
   if (!plan.ntiles) return cudaSuccess;
   gemm_tcg_kernel<<<plan.grid, kTgThreads, tcg_smem_bytes(), s>>>(
-      plan.d_probs, reinterpret_cast<const CUtensorMap *>(plan.d_maps), plan.d_tiles, plan.ntiles, plan.nprob, err);
+      plan.d_probs, reinterpret_cast<const CUtensorMap *>(plan.d_maps), plan.d_tiles, plan.ntiles, plan.nprob, err,
+      out0);
   count_launch();
   return cudaGetLastError();
 }

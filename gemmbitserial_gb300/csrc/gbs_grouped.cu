@@ -350,6 +350,8 @@ int gbs_group_gemm(gbs_group *g, void *stream) {
   cudaError_t e = cudaSuccess;
   if (digits_stale(g)) e = tcg_expand(g->tc, (cudaStream_t)stream);
   if (e == cudaSuccess) e = enqueue_gemm(g, (cudaStream_t)stream);
+  if (e == cudaSuccess)
+    for (gbs_ctx *c : g->ctxs) c->res_stale = false;
   return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_group_gemm");
 }
 
@@ -401,6 +403,7 @@ int gbs_group_replay(gbs_group *g, void *stream) {
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_replay");
   if (g->npack)  // the replay packs new planes: cached adjoint operands are stale
     for (gbs_ctx *c : g->ctxs) c->vt_valid[0] = c->vt_valid[1] = false;
+  for (gbs_ctx *c : g->ctxs) c->res_stale = false;
   count_launch(g->launches_per_replay);
   return GBS_OK;
 }

@@ -140,6 +140,10 @@ struct gbs_ctx {
   gbs::Mat lhs, rhs;
   uint64_t lhsBlock = 0, rhsBlock = 0;
   int32_t *res = nullptr;     // [N][M]
+  // result target of the forward launch being issued: res, or a caller's
+  // buffer the device can write (gbs_gemm_to); res is stale after the latter
+  int32_t *out = nullptr;
+  bool res_stale = false;
   int32_t *rowsum = nullptr;  // scratch: row sums, lhs rows at [0, M), rhs rows at [M, M+N)
   // host-source imports: per-side device staging, a copy stream and events
   // that let the packing of each copied chunk overlap the copy of the next
@@ -173,6 +177,9 @@ struct gbs_ctx {
 };
 
 namespace gbs {
+
+// where the forward kernels of this context write the result
+inline int32_t *result_ptr(const gbs_ctx *c) { return c->out ? c->out : c->res; }
 
 // epilogue of one context (gbs_api.cu)
 void make_epilogue(const gbs_ctx *c, Epilogue &e, int32_t *rowsum);
@@ -233,7 +240,7 @@ bool tcg_preferred(const gbs_ctx *c);
 int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n);
 void tcg_plan_free(TcgPlan *plan);
 cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s);
-cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s);
+cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s, int32_t *out0 = nullptr);
 cudaError_t ensure_digit_buffer(gbs_ctx *c, int side);
 // tensor-core adjoint (gbs_adjoint_tc.cu)
 int adjoint_tc(gbs_ctx *c, const float *dC, float *dA, float *dB, cudaStream_t s);

@@ -111,9 +111,12 @@ GBS_API int gbs_ctx_get_info(const gbs_ctx *ctx, gbs_ctx_info *info);
  * its uint8_t overload (:249-275) for ctx.lhs (side 0, M x K) or ctx.rhs
  * (side 1, N x K, i.e. B transposed).  src is row-major [rows][K], or
  * [K][rows] when col_major (the reference's readColMajor).  src may be host
- * memory (pageable or pinned) or device memory; host data is copied to the
- * device first.  The packing runs on `stream`; with host src the call returns
- * once src may be reused. */
+ * memory (pageable or pinned) or device memory.  Host data the device can
+ * address (pinned, or pageable where the GPU walks the host page tables) is
+ * packed in place over the host link; other host data is copied to the
+ * device first, in chunks whose packing overlaps the next copy.
+ * GBS_HOST_DIRECT=0 in the environment forces the copies.  The packing runs
+ * on `stream`; with host src the call returns once src may be reused. */
 GBS_API int gbs_import(gbs_ctx *ctx, int side, const void *src, int dtype, int col_major, void *stream);
 
 /* Replaces BitSerialMatrix::importRegularAndQuantize<T> (gemmbitserial.hpp:
@@ -135,6 +138,17 @@ GBS_API int gbs_import_quantize(gbs_ctx *ctx, int side, const void *src, const v
  * res[n*M + m], bit-exact with the reference (int32 with wrap-around).
  * Asynchronous on `stream`. */
 GBS_API int gbs_gemm(gbs_ctx *ctx, void *stream);
+
+/* gemmBitSerial followed by the read of ctx.res (gemmbitserial.hpp:383), as
+ * the reference's callers do it, fused: the forward kernels write the N x M
+ * result straight into dst (M*N int32) when dst is device or pinned host
+ * memory, 16-byte aligned, so the transfer over the host link overlaps the
+ * GEMM instead of following it.  Otherwise (pageable or unaligned dst) it
+ * runs gbs_gemm and copies.  With host dst the
+ * call returns after the result has landed.  A direct write leaves the
+ * context's own device result stale: gbs_get_result then fails with
+ * GBS_ESTATE until the next gbs_gemm. */
+GBS_API int gbs_gemm_to(gbs_ctx *ctx, int32_t *dst, void *stream);
 
 /* Copies the result (ctx.res in the reference, gemmbitserial.hpp:383) to dst,
  * host or device memory of M*N int32.  With host dst the call returns after

@@ -206,7 +206,7 @@ inline GEMMContext allocGEMMContext(uint64_t lhsRows, uint64_t depth, uint64_t r
   detail::check(gbs_ctx_get_info(c, &info));
   g.lhsBlock = info.lhsBlock;
   g.rhsBlock = info.rhsBlock;
-  g.res = new int32_t[lhsRows * rhsRows + 1];
+  g.res = new int32_t[lhsRows * rhsRows + 1]();  // zeroed: its pages exist before the device writes them
   return g;
 }
 
@@ -217,11 +217,9 @@ inline GEMMContext allocateGEMMContext(uint64_t lhsRows, uint64_t depth, uint64_
 }
 
 // gemmBitSerial (reference arch-generic.hpp:331-345): runs on the GPU and
-// leaves the result in ctx.res when it returns.
-inline void gemmBitSerial(GEMMContext ctx) {
-  detail::check(gbs_gemm(ctx.handle, nullptr));
-  detail::check(gbs_get_result(ctx.handle, ctx.res, nullptr));
-}
+// leaves the result in ctx.res when it returns.  The kernels write ctx.res
+// over the host link themselves where the device can address it.
+inline void gemmBitSerial(GEMMContext ctx) { detail::check(gbs_gemm_to(ctx.handle, ctx.res, nullptr)); }
 
 // deallocGEMMContext (reference gemmbitserial.hpp:454-458).
 inline void deallocGEMMContext(GEMMContext ctx) {
