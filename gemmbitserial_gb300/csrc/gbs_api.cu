@@ -185,6 +185,13 @@ uint64_t gbs_debug_launch_count(void) { return g_launches.load(); }
 
 uint32_t gbs_debug_tc_error(void) { return tc_error_word(); }
 
+int gbs_debug_last_pair(const gbs_ctx *c, int *bn, int *splits) {
+  if (!c || !bn || !splits) return fail(GBS_EINVAL, "gbs_debug_last_pair: NULL argument");
+  *bn = c->last_pair_bn;
+  *splits = c->last_pair_splits;
+  return GBS_OK;
+}
+
 int gbs_tc_peaks(double *f8_flops, double *bf16_flops) { return tc_peaks(f8_flops, bf16_flops); }
 
 int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB,
@@ -552,8 +559,9 @@ int gbs_clear(gbs_ctx *c, int side, void *stream) {
 
 int gbs_set_variant(gbs_ctx *c, int variant) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_variant: ctx is NULL");
-  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256 || variant == kPairVariant))
-    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128, 256 or 512");
+  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256 || variant == kPairVariant ||
+        variant == kPairVariant128))
+    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128, 256, 512 or 513");
   c->variant = variant;
   return GBS_OK;
 }

@@ -28,7 +28,9 @@
 // stops issuing work, waits (bounded) for what it issued and frees TMEM.
 #include <cuda.h>
 
+#include <chrono>
 #include <cstring>
+#include <thread>
 
 #include "gbs_internal.h"
 #include "gbs_tc_common.cuh"
@@ -338,9 +340,9 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
         if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) break;
         mbar_expect_tx(full + 8 * s, stage_bytes);
         const uint32_t dst = smem_u32(smem + s * stage_bytes);
-        tma_load_2d(dst, &tmA, (int)(k * 128), (int)m0, full + 8 * s);
+        tma_load_digits(dst, &tmA, (int)k, (uint32_t)m0, full + 8 * s);
         for (int h = 0; h < BN / 128; h++)
-          tma_load_2d(dst + a_bytes + h * 128 * kRowB, &tmB, (int)(k * 128), (int)(n0 + 128 * h), full + 8 * s);
+          tma_load_digits(dst + a_bytes + h * 128 * kRowB, &tmB, (int)k, (uint32_t)(n0 + 128 * h), full + 8 * s);
         issued = k + 1;
       }
       if (*abort_flag) {
@@ -405,12 +407,13 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
   }
 }
 
-// Pair kernel: a cluster of two CTAs on two SMs computes one 256 x 256
-// output tile with tcgen05.mma.cta_group::2 (M = 256, N = 256, K = 32).
-// CTA rank r holds A rows [m0 + 128r, +128) and B rows [n0 + 128r, +128) of
-// every stage and accumulates its 128 result rows x 256 columns in its own
-// TMEM, so each SM receives 32 KB per 128-digit stage for the math a 1-SM
-// 128 x 256 tile does with 48 KB.
+// Pair kernel: a cluster of two CTAs on two SMs computes one 256 x BN
+// output tile (BN = 256 or 128) with tcgen05.mma.cta_group::2 (M = 256,
+// N = BN, K = 32).  CTA rank r holds A rows [m0 + 128r, +128) and B rows
+// [n0 + BN/2 r, +BN/2) of every stage and accumulates its 128 result rows x
+// BN columns in its own TMEM; at BN = 256 each SM receives 32 KB per
+// 128-digit stage for the math a 1-SM 128 x 256 tile does with 48 KB.  The
+// 128-column tiles double the tile count for shapes with few tiles.
 //   warp 0     TMA of this CTA's halves; both CTAs signal the full barrier of
 //              rank 0 (the leader), which expects the bytes of both
 //   warp 1     TMEM allocation (both CTAs, collectively); in the leader, lane
@@ -419,7 +422,7 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 //   warps 2-5  epilogue of this CTA's 128 rows
 // A cluster barrier closes the kernel, so no CTA frees TMEM or exits while
 // its peer may still signal its barriers or write its accumulator.
-constexpr int kPairStagesMax = 7;
+constexpr int kPairStagesMax = 9;
 constexpr size_t kPairSmemCap = 227 * 1024;  // the per-block dynamic shared memory limit
 constexpr int kPairThreads = 192;
 constexpr uint32_t kPairHalfBytes = 128 * kRowB;  // 128 rows x 128 digits
@@ -434,11 +437,13 @@ __device__ __forceinline__ uint32_t map_to_rank(uint32_t smem_addr, uint32_t ran
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(smem_addr), "r"(rank));
   return d;
 }
-__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+// tma_load_digits for an SM pair: completes on `bar`, the leader CTA's barrier.
+__device__ __forceinline__ void tma_load_digits_pair(uint32_t dst, const CUtensorMap *map, int k, uint32_t row,
+                                                     uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
-      "%3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
+      "%3, %4, %5}], [%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(k), "r"((int)(row >> 4)), "r"(bar)
       : "memory");
 }
 __device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -496,7 +501,7 @@ __device__ __forceinline__ void store_cols(const TmaArgs &a, const uint32_t (&v)
   }
 }
 
-template <int SPLITS>
+template <int SPLITS, int BN>
 __global__ void __launch_bounds__(kPairThreads, 1)
     gemm_tc_pair_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TmaArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -506,13 +511,14 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   // ranks 2p and 2p+1 form the SM pair of K chunk p; the even one leads
   const uint32_t peer = rank & 1u, split = rank >> 1, lead = rank & ~1u;
   const uint16_t pair_mask = (uint16_t)(3u << lead);
-  const uint32_t stage_bytes = 2 * kPairHalfBytes;
+  constexpr uint32_t kBHalf = (BN / 2) * kRowB;  // this CTA's BN/2 rows of the B tile
+  const uint32_t stage_bytes = kPairHalfBytes + kBHalf;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.stages * stage_bytes);
   const uint32_t full = smem_u32(bars), empty = full + 8 * a.stages, acc_full = empty + 8 * a.stages;
   const uint32_t mma_done = acc_full + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * a.stages + 2);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
-  const uint64_t pair_m0 = (uint64_t)(blockIdx.x / (2 * SPLITS)) * 256, n0 = (uint64_t)blockIdx.y * 256;
+  const uint64_t pair_m0 = (uint64_t)(blockIdx.x / (2 * SPLITS)) * 256, n0 = (uint64_t)blockIdx.y * BN;
   const uint64_t m0 = pair_m0 + 128 * peer;
   const uint32_t k_lo = split * a.nstages / SPLITS, k_hi = (split + 1) * a.nstages / SPLITS;
   const uint32_t nk = k_hi - k_lo;
@@ -530,7 +536,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "n"(256));
+                 "n"(BN));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -549,8 +555,8 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         const uint32_t fb = map_to_rank(full + 8 * s, lead);
         if (peer == 0) mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
         const uint32_t dst = smem_u32(smem + s * stage_bytes);
-        tma_load_2d_pair(dst, &tmA, (int)((k_lo + k) * 128), (int)m0, fb);
-        tma_load_2d_pair(dst + kPairHalfBytes, &tmB, (int)((k_lo + k) * 128), (int)(n0 + 128 * peer), fb);
+        tma_load_digits_pair(dst, &tmA, (int)(k_lo + k), (uint32_t)m0, fb);
+        tma_load_digits_pair(dst + kPairHalfBytes, &tmB, (int)(k_lo + k), (uint32_t)(n0 + (BN / 2) * peer), fb);
         issued = k + 1;
       }
       // After an abort the leader waits (bounded) for the loads its barriers
@@ -602,7 +608,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         // one 32-column TMEM load at a time (measured faster than keeping the
         // next load in flight during the stores)
 #pragma unroll 1
-        for (int col = 0; col < 256; col += 32) {
+        for (int col = 0; col < BN; col += 32) {
           uint32_t v[32];
           tmem_ld32(taddr + (uint32_t)col, v);
           tmem_wait_ld(v);
@@ -614,9 +620,9 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         // and later reads remotely, 16 bytes per quad, a warp 512 contiguous
         // bytes; this chunk's own columns stay in TMEM
         float4 *part = reinterpret_cast<float4 *>(smem) + q * 32 + lane;
-        const uint32_t own0 = split * (256u / SPLITS), own1 = own0 + 256u / SPLITS;
+        const uint32_t own0 = split * (BN / SPLITS), own1 = own0 + BN / SPLITS;
 #pragma unroll 1
-        for (uint32_t col = 0; col < 256; col += 32) {
+        for (uint32_t col = 0; col < BN; col += 32) {
           if (col >= own0 && col < own1) continue;
           uint32_t v[32];
           tmem_ld32(taddr + (uint32_t)col, v);
@@ -634,13 +640,13 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
   if constexpr (SPLITS > 1) {
     // Split-K reduction over distributed shared memory: the CTA of chunk p sums
-    // columns [p*256/S, (p+1)*256/S) of its 128 rows over the S partial tiles
+    // columns [p*BN/S, (p+1)*BN/S) of its 128 rows over the S partial tiles
     // (integers below 2^24: the fp32 sums are exact) and stores them; a warp's
     // remote loads and its stores each cover 32 consecutive rows of a column.
     if (warp >= 2 && tile_done) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int q = warp & 3;
-      const uint32_t row = (uint32_t)(q * 32 + lane), cols = 256u / SPLITS, c0 = split * cols;
+      const uint32_t row = (uint32_t)(q * 32 + lane), cols = BN / SPLITS, c0 = split * cols;
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + c0;
       const uint64_t gm = m0 + row;
       const float4 *mine = reinterpret_cast<const float4 *>(smem) + (c0 >> 2) * 128 + row;
@@ -678,25 +684,27 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;");
-    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(256));
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(BN));
   }
 }
 
 // Throughput probe: one CTA per SM, one thread issuing back-to-back
-// tcgen05.mma (M=128, N=256) from fixed zeroed shared tiles; kind 0 = e4m3
-// (K=32), kind 1 = bf16 (K=16).  A commit + bounded wait closes every 64 MMAs.
-__global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters, int kind) {
+// tcgen05.mma (M=128, N=256) from fixed zeroed shared tiles; KIND 0 = e4m3
+// (K=32), KIND 1 = bf16 (K=16).  A commit + bounded wait closes every 64
+// MMAs.  The issue loop holds nothing but the MMAs: one thread's issue rate
+// is close to the tensor core's, and a runtime branch per MMA measurably
+// lowered the rate it reported.
+template <int KIND>
+__global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + 48 * 1024);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   for (int i = threadIdx.x; i < 48 * 1024 / 16; i += blockDim.x)
     reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (threadIdx.x == 0) {
     mbar_init(smem_u32(bar), 1);
-    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (threadIdx.x < 32) {
@@ -709,7 +717,7 @@ __global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters, int kind) {
   const uint32_t tmem = *tmem_slot;
   if (threadIdx.x == 0) {
     const uint32_t a0 = smem_u32(smem), b0 = a0 + 16 * 1024;
-    const uint32_t idesc = (1u << 4) | (kind ? ((1u << 7) | (1u << 10)) : 0u) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+    const uint32_t idesc = (1u << 4) | (KIND ? ((1u << 7) | (1u << 10)) : 0u) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
     uint32_t phase = 0;
     for (int it = 0; it < iters; it++) {
 #pragma unroll 1
@@ -717,7 +725,7 @@ __global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters, int kind) {
 #pragma unroll
         for (int kk = 0; kk < 4; kk++) {
           const uint64_t ad = sw128_desc(a0 + kk * 32), bd = sw128_desc(b0 + kk * 32);
-          if (kind)
+          if constexpr (KIND == 1)
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -726,7 +734,12 @@ __global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters, int kind) {
             mma_f8(tmem, ad, bd, idesc, 1u);
         }
       mma_commit(smem_u32(bar));
-      if (!mbar_wait(smem_u32(bar), phase, abort_flag)) break;
+      bool done = false;
+      for (uint32_t w = 0; w < kTcWaitLimit && !done; ++w) done = mbar_try(smem_u32(bar), phase);
+      if (!done) {
+        atomicOr(&g_tc_error, 2u);
+        break;
+      }
       phase ^= 1;
     }
   }
@@ -821,14 +834,17 @@ size_t tc_smem(int ntA, int ntB, int wa, int wb, int bn, int no) {
 
 }  // namespace
 
+// Map of a digit matrix (rows x cols, 16-row blocks: digit_offset) as the
+// 4-D tensor [rows/16][cols/128][16][128] bytes; a box is box_rows rows (a
+// multiple of 16, <= 256) of one 128-digit column chunk, 128-byte swizzled.
 bool tc_map_u8(void *map, const uint8_t *base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn();
-  if (!fn || box_rows == 0 || box_rows > 256) return false;
-  cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {cols};
-  cuuint32_t box[2] = {128, box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void *)base, dims, strides, box,
+  if (!fn || box_rows == 0 || box_rows > 256 || box_rows % 16 || cols % 128 || rows % 16) return false;
+  cuuint64_t dims[4] = {128, 16, cols / 128, rows / 16};
+  cuuint64_t strides[3] = {128, 2048, (cols / 128) * 2048};
+  cuuint32_t box[4] = {128, 16, 1, box_rows / 16};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 4, (void *)base, dims, strides, box,
             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -906,16 +922,8 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn_req) 
 namespace {
 
 // Tensor map over a digit matrix: 2-D u8 [nrows_a][ncols_a], box 128 x 128, 128-byte swizzle.
-bool make_digit_map(CUtensorMap *map, const uint8_t *digits, const Mat &m) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return false;
-  cuuint64_t dims[2] = {m.ncols_a, m.nrows_a};
-  cuuint64_t strides[1] = {m.ncols_a};
-  cuuint32_t box[2] = {128, 128};
-  cuuint32_t estr[2] = {1, 1};
-  return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void *)digits, dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+bool make_digit_map(CUtensorMap *map, const uint8_t *digits, const Mat &m, uint32_t box_rows = 128) {
+  return tc_map_u8(map, digits, m.ncols_a, m.nrows_a, box_rows);
 }
 
 cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
@@ -930,23 +938,48 @@ cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
 
 namespace {
 
-size_t pair_smem_bytes() {
-  const size_t stage_bytes = 2 * kPairHalfBytes;
+int sm_count_cached() {
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  if (!cache[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) cudaGetLastError();
+    cache[dev] = v > 0 ? v : 1;
+  }
+  return cache[dev];
+}
+
+// Stages of the pair kernel's ring for BN-column tiles, and its shared memory.
+int pair_stages(int bn) {
+  const size_t stage_bytes = kPairHalfBytes + (size_t)(bn / 2) * kRowB;
   int stages = kPairStagesMax;
   while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 > kPairSmemCap) stages--;
-  return 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16;
+  return stages;
+}
+size_t pair_smem_bytes(int bn) {
+  const int stages = pair_stages(bn);
+  return 1024 + stages * (kPairHalfBytes + (size_t)(bn / 2) * kRowB) + 8 * (2 * stages + 2) + 16;
 }
 
-template <int S>
-void pair_set_attrs(size_t smem) {
-  cudaFuncSetAttribute(gemm_tc_pair_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+// Calls f with the kernel instance of `splits` and `bn` (1/2/4 x 256/128).
+template <typename F>
+cudaError_t with_pair_kernel(int splits, int bn, F f) {
+  if (bn == 128) {
+    if (splits == 4) return f(gemm_tc_pair_kernel<4, 128>);
+    if (splits == 2) return f(gemm_tc_pair_kernel<2, 128>);
+    return f(gemm_tc_pair_kernel<1, 128>);
+  }
+  if (splits == 4) return f(gemm_tc_pair_kernel<4, 256>);
+  if (splits == 2) return f(gemm_tc_pair_kernel<2, 256>);
+  return f(gemm_tc_pair_kernel<1, 256>);
 }
 
-void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1], int splits, size_t smem,
+void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1], int splits, int bn, size_t smem,
                         cudaStream_t s) {
-  if (splits == 4) pair_set_attrs<4>(smem);
-  else if (splits == 2) pair_set_attrs<2>(smem);
-  else pair_set_attrs<1>(smem);
+  with_pair_kernel(splits, bn, [&](auto kern) {
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  });
   memset(&cfg, 0, sizeof(cfg));
   cfg.blockDim = dim3(kPairThreads);
   cfg.dynamicSmemBytes = smem;
@@ -961,20 +994,18 @@ void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1],
 
 // Clusters of 2 * splits CTAs that fit the GPU at once (they are placed within
 // one GPC each), cached per device.
-int pair_max_clusters(int splits) {
-  static int cache[64][5] = {};
+int pair_max_clusters(int splits, int bn) {
+  static int cache[64][5][2] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  int &v = cache[dev][splits];
+  int &v = cache[dev][splits][bn == 128 ? 1 : 0];
   if (v == 0) {
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    pair_launch_config(cfg, attr, splits, pair_smem_bytes(), nullptr);
+    pair_launch_config(cfg, attr, splits, bn, pair_smem_bytes(bn), nullptr);
     cfg.gridDim = dim3(2 * splits, 1, 1);
     int n = 0;
-    cudaError_t e;
-    if (splits == 4) e = cudaOccupancyMaxActiveClusters(&n, gemm_tc_pair_kernel<4>, &cfg);
-    else e = cudaOccupancyMaxActiveClusters(&n, gemm_tc_pair_kernel<2>, &cfg);
+    cudaError_t e = with_pair_kernel(splits, bn, [&](auto kern) { return cudaOccupancyMaxActiveClusters(&n, kern, &cfg); });
     if (e != cudaSuccess) {
       cudaGetLastError();
       n = 0;
@@ -982,6 +1013,14 @@ int pair_max_clusters(int splits) {
     v = n > 0 ? n : -1;
   }
   return v > 0 ? v : 0;
+}
+
+// K split of a grid of `tiles` pair tiles: the largest of 4 or 2 that keeps
+// >= 8 stages per chunk and fits one wave, else 1.
+int pair_splits(uint64_t tiles, uint32_t nstages, int bn) {
+  for (int cand : {4, 2})
+    if (nstages / cand >= 8 && tiles <= (uint64_t)pair_max_clusters(cand, bn)) return cand;
+  return 1;
 }
 
 }  // namespace
@@ -1017,34 +1056,45 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     if (!err) return cudaErrorInvalidSymbol;
     return tcg_gemm(*c->plan1, err, s, c->out);
   }
-  if (bn_req == kPairVariant || bn_req < 0) {  // 256 x 256 tiles on SM pairs
-    a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+  if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req < 0) {  // 256 x BN tiles on SM pairs
     // Split K over up to 4 SM pairs per tile (a cluster of up to 8 CTAs) while
     // the grid still fits one wave and every chunk keeps >= 8 stages: shapes
-    // with few output tiles and a long K then use the whole GPU.
-    const uint64_t pair_tiles = ((a.M + 255) / 256) * ((a.N + 255) / 256);
-    a.splits = 1;
-    for (int cand : {4, 2})
-      if (a.nstages / cand >= 8 && pair_tiles <= (uint64_t)pair_max_clusters(cand)) {
-        a.splits = cand;
-        break;
+    // with few output tiles and a long K then use the whole GPU.  128-column
+    // tiles are taken where 256-column ones, split, would still leave more
+    // than half of the SM pairs idle and the narrower tiles occupy more.
+    const uint64_t mt = (a.M + 255) / 256;
+    int bn = bn_req == kPairVariant128 ? 128 : 256;
+    int splits = pair_splits(mt * ((a.N + bn - 1) / bn), a.nstages, bn);
+    if (bn_req < 0) {
+      const uint64_t pairs = (uint64_t)sm_count_cached() / 2;
+      const uint64_t used256 = mt * ((a.N + 255) / 256) * splits;
+      const int s128 = pair_splits(mt * ((a.N + 127) / 128), a.nstages, 128);
+      const uint64_t tiles128 = mt * ((a.N + 127) / 128);
+      const uint64_t used128 = tiles128 * s128;
+      if (2 * used256 < pairs && used128 > used256 && used128 <= pairs) {
+        bn = 128;
+        splits = s128;
       }
-    const size_t stage_bytes = 2 * kPairHalfBytes;
-    int stages = kPairStagesMax;
-    while (stages > 2 && 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16 > kPairSmemCap) stages--;
-    a.stages = stages;
-    const size_t smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 2) + 16;
+    }
+    if (bn == 128 && !c->digit_map_b64_ready) {
+      if (!make_digit_map(reinterpret_cast<CUtensorMap *>(c->tc_map_db64), c->digits[1], c->rhs, 64))
+        return cudaErrorInvalidValue;
+      c->digit_map_b64_ready = true;
+    }
+    a.splits = splits;
+    a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+    a.stages = pair_stages(bn);
+    const size_t smem = pair_smem_bytes(bn);
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
-    pair_launch_config(cfg, attr, a.splits, smem, s);
-    cfg.gridDim = dim3((unsigned)(2 * a.splits * ((a.M + 255) / 256)), (unsigned)((a.N + 255) / 256));
+    pair_launch_config(cfg, attr, a.splits, bn, smem, s);
+    cfg.gridDim = dim3((unsigned)(2 * a.splits * mt), (unsigned)((a.N + bn - 1) / bn));
     const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
-    const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_db);
-    cudaError_t e;
-    if (a.splits == 4) e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel<4>, ma, mb, a);
-    else if (a.splits == 2) e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel<2>, ma, mb, a);
-    else e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_kernel<1>, ma, mb, a);
+    const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(bn == 128 ? c->tc_map_db64 : c->tc_map_db);
+    cudaError_t e = with_pair_kernel(a.splits, bn, [&](auto kern) { return cudaLaunchKernelEx(&cfg, kern, ma, mb, a); });
     count_launch();
+    c->last_pair_bn = bn;
+    c->last_pair_splits = a.splits;
     return e != cudaSuccess ? e : cudaGetLastError();
   }
   const int bn = (bn_req == 128 || bn_req == 256) ? bn_req : (a.N > 128 ? 256 : 128);
@@ -1072,36 +1122,50 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   return cudaGetLastError();
 }
 
-// Sustained tcgen05 MMA rate in FLOP/s (2 per multiply-add) for e4m3 and bf16.
+// tcgen05 MMA rate in FLOP/s (2 per multiply-add) for e4m3 and bf16 at full
+// SM clock: the best of several ~0.2 ms bursts, each too short for the power
+// limit to pull the clock down (longer loops settle ~25 % lower on a
+// 1.4 kW GB300).  The kernels it is the ceiling of run for tens of
+// microseconds at a time, at full clock.
 int tc_peaks(double *f8, double *bf16) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t smem = 1024 + 48 * 1024 + 64;
-  cudaError_t e = cudaFuncSetAttribute(peak_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(peak_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(peak_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_tc_peaks");
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   double out[2] = {0, 0};
-  const int iters = 200;
+  // rate from the difference of a short and a long burst (launch cost cancels),
+  // best of several, with idle gaps so the power draw stays low between them
+  const int lo = 20, hi = 60;
   for (int kind = 0; kind < 2; kind++) {
-    peak_tc_kernel<<<sms, 128, smem>>>(4, kind);
+    auto launch = [&](int iters) {
+      if (kind) peak_tc_kernel<1><<<sms, 128, smem>>>(iters);
+      else peak_tc_kernel<0><<<sms, 128, smem>>>(iters);
+    };
+    launch(4);
     cudaDeviceSynchronize();
-    float best = 1e30f;
-    for (int r = 0; r < 3; r++) {
-      cudaEventRecord(e0);
-      peak_tc_kernel<<<sms, 128, smem>>>(iters, kind);
-      cudaEventRecord(e1);
-      cudaEventSynchronize(e1);
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      if (ms < best) best = ms;
-    }
-    const double k = kind ? 16.0 : 32.0;
-    out[kind] = 2.0 * sms * (double)iters * 64.0 * 128.0 * 256.0 * k / (best * 1e-3);
+    float best[2] = {1e30f, 1e30f};
+    for (int r = 0; r < 6; r++)
+      for (int v = 0; v < 2; v++) {
+        std::this_thread::sleep_for(std::chrono::milliseconds(1));
+        cudaEventRecord(e0);
+        launch(v ? hi : lo);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best[v] = std::min(best[v], ms);
+      }
+    const double k = kind ? 16.0 : 32.0, dt = (double)(best[1] - best[0]);
+    out[kind] = dt > 0 ? 2.0 * sms * (double)(hi - lo) * 64.0 * 128.0 * 256.0 * k / (dt * 1e-3) : 0.0;
   }
-  count_launch(8);
+  count_launch(26);
   e = cudaGetLastError();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -118,8 +118,8 @@ __global__ void __launch_bounds__(kTgThreads, 1)
           }
           mbar_expect_tx(full + 8 * s, bytes);
           const uint32_t dst = smem_u32(smem + s * kTgSlotBytes);
-          tma_load_2d(dst, ma, (int)(k * 128), (int)(tl.r * 128), full + 8 * s);
-          tma_load_2d(dst + kTgABytes, mb, (int)(k * 128), (int)(tl.c * P.bn), full + 8 * s);
+          tma_load_digits(dst, ma, (int)k, tl.r * 128, full + 8 * s);
+          tma_load_digits(dst + kTgABytes, mb, (int)k, tl.c * P.bn, full + 8 * s);
         }
       }
       if (*abort_flag)
@@ -256,7 +256,7 @@ __device__ __forceinline__ void expand_chunk(const ExpandJob &j, uint32_t r, uin
     const uint32_t c0 = col0 + 4 * n;
     if (c0 + 4 > j.K) q[n] &= c0 >= j.K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (j.K - c0))));
   }
-  *reinterpret_cast<uint4 *>(j.digits + (uint64_t)r * j.ncols_a + col0) = make_uint4(q[0], q[1], q[2], q[3]);
+  *reinterpret_cast<uint4 *>(j.digits + digit_offset(r, col0, j.ncols_a)) = make_uint4(q[0], q[1], q[2], q[3]);
 }
 
 __device__ __forceinline__ void expand_thread(const ExpandJob &j, uint64_t local) {
@@ -349,6 +349,7 @@ cudaError_t ensure_digit_buffer(gbs_ctx *c, int side) {
   if (e == cudaSuccess) e = cudaMemset(c->digits[side], 0, bytes);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   c->digit_maps_ready = false;
+  c->digit_map_b64_ready = false;
   c->plan1_ready = false;
   c->digits_valid[side] = false;
   return e;

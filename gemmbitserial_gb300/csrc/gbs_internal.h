@@ -16,6 +16,15 @@ constexpr uint64_t kRowAlign = 256;  // device row padding (rows of a plane): a 
 constexpr uint64_t kColAlign = 256;  // device column padding (bits of a row)
 constexpr int kMaxBits = 8;
 
+// e4m3 digit matrices (the tensor-core pipe's operands) are stored in 16-row
+// blocks: each 16-row x 128-digit tile is 2 KB contiguous, laid out
+// [row/16][col/128][row%16][col%128].  A TMA box of an operand tile then
+// reads runs of 2 KB instead of 128-byte row pieces ncols_a bytes apart,
+// which HBM serves at a far higher rate for the long-K, many-row operands.
+__host__ __device__ inline uint64_t digit_offset(uint64_t r, uint64_t col, uint64_t ncols_a) {
+  return ((r >> 4) * (ncols_a >> 7) + (col >> 7)) * 2048 + ((r & 15) << 7) + (col & 127);
+}
+
 // One bit-serial matrix on the device: planes [nbits][nrows_a][wpr] of u64.
 struct Mat {
   uint64_t nbits = 0, nrows = 0, ncols = 0, nrows_a = 0, ncols_a = 0;
@@ -169,6 +178,9 @@ struct gbs_ctx {
   alignas(64) unsigned char tc_map_da[128];
   alignas(64) unsigned char tc_map_db[128];
   bool digit_maps_ready = false;
+  alignas(64) unsigned char tc_map_db64[128];  // rhs digits in 64-row boxes (the pair kernel's 128-column tiles)
+  bool digit_map_b64_ready = false;
+  int last_pair_bn = 0, last_pair_splits = 0;  // configuration of the last SM-pair launch (test hook)
   // one-problem plan of the persistent tensor-core kernel (shapes with a side under 256 rows)
   gbs::TcgPlan *plan1 = nullptr;
   bool plan1_ready = false;
@@ -224,7 +236,8 @@ bool tc_exact(const gbs_ctx *c, int pipe);
 uint32_t *tc_error_ptr();
 cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
-constexpr int kPairVariant = 512;  // tensor-core variant: 256 x 256 tiles on SM pairs (tcgen05 cta_group::2)
+constexpr int kPairVariant = 512;     // tensor-core variant: 256 x 256 tiles on SM pairs (tcgen05 cta_group::2)
+constexpr int kPairVariant128 = 513;  // the same with 256 x 128 tiles
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 

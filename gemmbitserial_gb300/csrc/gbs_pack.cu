@@ -119,7 +119,7 @@ __device__ __forceinline__ uint32_t digits4(uint32_t x, int nbits, uint4 tab) {
 }
 
 // The lane's 32 digits of padded row r (0 past nrows and past ncols) into the
-// digit matrix [nrows_a][64 * wpr].
+// digit matrix (64 * wpr columns, 16-row blocks: digit_offset).
 __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int nbits, uint64_t nrows,
                                                uint64_t ncols, uint64_t wpr, uint4 tab, uint64_t r, uint64_t col0,
                                                const uint32_t (&q)[8]) {
@@ -133,7 +133,7 @@ __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int
       if (c + 4 > ncols) d[i] &= c >= ncols ? 0u : (0xFFFFFFFFu >> (8 * (4 - (ncols - c))));
     }
   }
-  uint4 *dst = reinterpret_cast<uint4 *>(digits + r * wpr * 64 + col0);
+  uint4 *dst = reinterpret_cast<uint4 *>(digits + digit_offset(r, col0, wpr * 64));
   dst[0] = make_uint4(d[0], d[1], d[2], d[3]);
   dst[1] = make_uint4(d[4], d[5], d[6], d[7]);
 }

@@ -297,6 +297,7 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
     cands[nc++] = Cand{GBS_PIPE_TC, 128};
     cands[nc++] = Cand{GBS_PIPE_TC, 256};
     cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant};
+    cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant128};
   }
   if (tc_exact(c, GBS_PIPE_TC_SMEM)) {
     cands[nc++] = Cand{GBS_PIPE_TC_SMEM, 256};

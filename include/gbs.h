@@ -186,9 +186,11 @@ GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);
 
 /* Forces the variant of a context's pipe: CUDA-core tile class (0: 64x64,
  * 1: 32x128, 2: 16x256 outputs per CTA), tensor-core N tile (128 or 256 rows
- * of rhs per 128-row lhs tile on one SM), or 512 for GBS_PIPE_TC: 256 x 256
- * tiles computed by pairs of SMs (tcgen05 cta_group::2, two-CTA clusters);
- * -1 restores the built-in rule.  No reference counterpart. */
+ * of rhs per 128-row lhs tile on one SM), or 512 / 513 for GBS_PIPE_TC:
+ * 256 x 256 / 256 x 128 tiles computed by pairs of SMs (tcgen05
+ * cta_group::2), K split over up to 4 pairs of one cluster when the tiles are
+ * too few to fill the GPU; -1 restores the built-in rule.  No reference
+ * counterpart. */
 GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
 
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
@@ -286,9 +288,11 @@ GBS_API int gbs_group_free(gbs_group *g);
  * No reference counterpart: the reference has a single CPU pipe. */
 GBS_API int gbs_pipe_peaks(double *popc_bitops, double *bmma_bitops);
 
-/* Measures the sustained tcgen05.mma rate (FLOP/s, 2 per multiply-add) of the
- * current device for e4m3 (kind::f8f6f4) and bf16 (kind::f16) operands with
- * an fp32 accumulator, M=128 N=256 (~10 ms).  No reference counterpart. */
+/* Measures the tcgen05.mma rate at full SM clock (FLOP/s, 2 per
+ * multiply-add) of the current device for e4m3 (kind::f8f6f4) and bf16
+ * (kind::f16) operands with an fp32 accumulator, M=128 N=256: short bursts,
+ * too short for the power limit to lower the clock (~30 ms in all).  No
+ * reference counterpart. */
 GBS_API int gbs_tc_peaks(double *f8_flops, double *bf16_flops);
 
 /* Measures the sustained FP32 FMA rate (FLOP/s, 2 per FMA) of the current
@@ -331,6 +335,10 @@ GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 
 /* Number of kernel launches the library has issued since load (all entry points). */
 GBS_API uint64_t gbs_debug_launch_count(void);
+
+/* Tile width (256 or 128) and K split (1, 2 or 4) of the last SM-pair kernel
+ * launched for ctx; both 0 if none was. */
+GBS_API int gbs_debug_last_pair(const gbs_ctx *ctx, int *bn, int *splits);
 
 #ifdef __cplusplus
 }

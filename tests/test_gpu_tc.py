@@ -2,6 +2,7 @@
 {0, +-2^i} operands, TMEM accumulation): bit-exact against the oracle and
 the reference's own full-size results, including sums up to just below 2^24
 (the exactness bound the pipe is selected under)."""
+import ctypes as C
 import hashlib
 import json
 import os
@@ -26,6 +27,7 @@ def lib(gbs_lib):
 
 
 PAIR = (_capi.GBS_PIPE_TC, 512)  # 256 x 256 tiles on SM pairs
+PAIR128 = (_capi.GBS_PIPE_TC, 513)  # 256 x 128 tiles on SM pairs
 
 
 def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True, pipe=_capi.GBS_PIPE_TC):
@@ -62,8 +64,8 @@ def test_tc_small_first():
 ENCS = [(1, "u"), (1, "b"), (2, "u"), (2, "s"), (3, "u"), (3, "s"), (4, "u"), (4, "s")]
 
 
-MODES = [_capi.GBS_PIPE_TC, PAIR, _capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS]
-MODE_IDS = ["hbm-digits", "hbm-digits-sm-pair", "smem-digits", "plane-pairs"]
+MODES = [_capi.GBS_PIPE_TC, PAIR, PAIR128, _capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS]
+MODE_IDS = ["hbm-digits", "hbm-digits-sm-pair", "hbm-digits-sm-pair-128", "smem-digits", "plane-pairs"]
 
 
 @pytest.mark.parametrize("mode", MODES, ids=MODE_IDS)
@@ -166,5 +168,60 @@ def test_tc_digit_cache_follows_reimport():
         ctx.lhs.importRegular(A2)
         gemmBitSerial(ctx)
         assert np.array_equal(ctx.res.reshape(N, M), O.oracle_gemm(A2, B, 2, 3, False, True))
+    finally:
+        deallocGEMMContext(ctx)
+
+
+def last_pair(ctx):
+    bn, sp = C.c_int(0), C.c_int(0)
+    _capi.check(_capi.load().gbs_debug_last_pair(ctx._h, C.byref(bn), C.byref(sp)))
+    return bn.value, sp.value
+
+
+# (variant, M, K, N, expected K split): 1, 2 and 4 pairs per tile at both tile widths
+SPLIT_CASES = [(512, 256, 8192, 256, 4), (512, 512, 2048, 512, 2), (512, 512, 512, 512, 1),
+               (513, 256, 8192, 256, 4), (513, 512, 2048, 512, 2), (513, 256, 512, 256, 1)]
+
+
+@pytest.mark.parametrize("case", SPLIT_CASES, ids=[f"v{c[0]}-{c[1]}x{c[2]}x{c[3]}" for c in SPLIT_CASES])
+def test_pair_split_k(case):
+    """The SM-pair kernel's in-cluster K split (partials summed over distributed shared memory)."""
+    variant, M, K, N, want_splits = case
+    rng = np.random.default_rng(M * 7 + K + N + variant)
+    for (wa, ea, wb, eb) in [(3, "u", 2, "s"), (1, "b", 1, "b"), (4, "s", 1, "b"), (2, "u", 1, "u")]:
+        A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+        B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+        sa, sb = ea != "u", eb != "u"
+        ctx = allocGEMMContext(M, K, N, wa, wb, sa, sb)
+        try:
+            _capi.check(_capi.load().gbs_set_variant(ctx._h, variant))
+            ctx.set_pipe(_capi.GBS_PIPE_TC)
+            assert ctx.pipe == _capi.GBS_PIPE_TC
+            ctx.lhs.importRegular(A)
+            ctx.rhs.importRegular(B)
+            gemmBitSerial(ctx)
+            got = ctx.res.reshape(N, M)
+            assert last_pair(ctx) == (256 if variant == 512 else 128, want_splits)
+        finally:
+            deallocGEMMContext(ctx)
+        assert np.array_equal(got, O.oracle_gemm(A, B, wa, wb, sa, sb)), (case, wa, ea, wb, eb)
+    assert _capi.load().gbs_debug_tc_error() == 0
+
+
+def test_pair_auto_fills_the_gpu_for_few_tiles():
+    """256 x 9216 x 4096 has 16 tiles of 256 x 256: the built-in rule narrows the tiles and/or
+    splits K so that at least half of the SM pairs work, bit-exact."""
+    import torch
+    pairs = torch.cuda.get_device_properties(0).multi_processor_count // 2
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload("gemm_256x9216x4096_bpbp")
+    ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    try:
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        gemmBitSerial(ctx)
+        assert sha(ctx.res.reshape(N, M)) == CFG["gemm_256x9216x4096_bpbp"]["sha256"]
+        bn, sp = last_pair(ctx)
+        assert bn in (128, 256) and sp >= 2 and (N // bn) * sp * 2 >= pairs, (bn, sp, pairs)
     finally:
         deallocGEMMContext(ctx)
