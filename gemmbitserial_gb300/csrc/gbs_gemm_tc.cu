@@ -414,8 +414,8 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
 // BN columns in its own TMEM; at BN = 256 each SM receives 32 KB per
 // 128-digit stage for the math a 1-SM 128 x 256 tile does with 48 KB.  The
 // 128-column tiles double the tile count for shapes with few tiles.
-//   warp 0     TMA of this CTA's halves; both CTAs signal the full barrier of
-//              rank 0 (the leader), which expects the bytes of both
+//   warp 0     in the leader: TMA of both CTAs' halves of every stage onto
+//              the leader's full barrier (the peer's into its shared memory)
 //   warp 1     TMEM allocation (both CTAs, collectively); in the leader, lane
 //              0 issues the MMAs and commits to the empty / accumulator
 //              barriers of both CTAs (multicast)
@@ -441,9 +441,9 @@ __device__ __forceinline__ uint32_t map_to_rank(uint32_t smem_addr, uint32_t ran
 __device__ __forceinline__ void tma_load_digits_pair(uint32_t dst, const CUtensorMap *map, int k, uint32_t row,
                                                      uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
-      "%3, %4, %5}], [%6];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(k), "r"((int)(row >> 4)), "r"(bar)
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
+      "%3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(k * 128), "r"((int)row), "r"(bar)
       : "memory");
 }
 __device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -547,29 +547,32 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    if (lane == 0) {
+    // The leader's TMA loads the stage for both CTAs: its own halves, and the
+    // peer's into the peer's shared memory, all completing on the leader's
+    // full barrier.  Each CTA loading its own halves onto that barrier puts a
+    // cross-SM completion on every stage's critical path, which measured about
+    // twice as slow per stage as the one-issuer ring.
+    if (lane == 0 && peer == 0) {
       uint32_t issued = 0;
       for (uint32_t k = 0; k < nk; k++) {
         const uint32_t s = k % a.stages, use = k / a.stages;
         if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) break;
         const uint32_t fb = map_to_rank(full + 8 * s, lead);
-        if (peer == 0) mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
-        const uint32_t dst = smem_u32(smem + s * stage_bytes);
-        tma_load_digits_pair(dst, &tmA, (int)(k_lo + k), (uint32_t)m0, fb);
-        tma_load_digits_pair(dst + kPairHalfBytes, &tmB, (int)(k_lo + k), (uint32_t)(n0 + (BN / 2) * peer), fb);
+        mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
+        const uint32_t dst = smem_u32(smem + s * stage_bytes), pdst = map_to_rank(dst, lead + 1);
+        const int kc = (int)(k_lo + k);
+        tma_load_digits_pair(dst, &tmA, kc, (uint32_t)pair_m0, fb);
+        tma_load_digits_pair(dst + kPairHalfBytes, &tmB, kc, (uint32_t)n0, fb);
+        tma_load_digits_pair(pdst, &tmA, kc, (uint32_t)(pair_m0 + 128), fb);
+        tma_load_digits_pair(pdst + kPairHalfBytes, &tmB, kc, (uint32_t)(n0 + BN / 2), fb);
         issued = k + 1;
       }
-      // After an abort the leader waits (bounded) for the loads its barriers
-      // expect.  The peer's loads complete on the leader's barriers, which the
-      // peer cannot wait on, so a stopped peer sleeps ~0.2 ms instead: far
-      // longer than a 16 KB load takes to land in its shared memory.
+      // after an abort, wait (bounded) for the loads the barriers still expect
+      // (the peer's shared memory is written until then; the closing cluster
+      // barrier keeps the peer resident)
       if (*abort_flag) {
-        if (peer == 0) {
-          for (uint32_t k = (issued > (uint32_t)a.stages ? issued - a.stages : 0); k < issued; k++)
-            mbar_drain(full + 8 * (k % a.stages), (k / a.stages) & 1);
-        } else {
-          for (int i = 0; i < 200; i++) __nanosleep(1000);
-        }
+        for (uint32_t k = (issued > (uint32_t)a.stages ? issued - a.stages : 0); k < issued; k++)
+          mbar_drain(full + 8 * (k % a.stages), (k / a.stages) & 1);
       }
     }
   } else if (warp == 1) {
@@ -834,17 +837,16 @@ size_t tc_smem(int ntA, int ntB, int wa, int wb, int bn, int no) {
 
 }  // namespace
 
-// Map of a digit matrix (rows x cols, 16-row blocks: digit_offset) as the
-// 4-D tensor [rows/16][cols/128][16][128] bytes; a box is box_rows rows (a
-// multiple of 16, <= 256) of one 128-digit column chunk, 128-byte swizzled.
+// 2-D map of a row-major digit matrix (rows x cols bytes); a box is box_rows
+// rows (<= 256) of one 128-digit column chunk, 128-byte swizzled.
 bool tc_map_u8(void *map, const uint8_t *base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn();
-  if (!fn || box_rows == 0 || box_rows > 256 || box_rows % 16 || cols % 128 || rows % 16) return false;
-  cuuint64_t dims[4] = {128, 16, cols / 128, rows / 16};
-  cuuint64_t strides[3] = {128, 2048, (cols / 128) * 2048};
-  cuuint32_t box[4] = {128, 16, 1, box_rows / 16};
-  cuuint32_t estr[4] = {1, 1, 1, 1};
-  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 4, (void *)base, dims, strides, box,
+  if (!fn || box_rows == 0 || box_rows > 256 || cols % 128) return false;
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols};
+  cuuint32_t box[2] = {128, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void *)base, dims, strides, box,
             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
