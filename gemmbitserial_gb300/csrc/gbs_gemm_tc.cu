@@ -441,9 +441,9 @@ __device__ __forceinline__ uint32_t map_to_rank(uint32_t smem_addr, uint32_t ran
 __device__ __forceinline__ void tma_load_digits_pair(uint32_t dst, const CUtensorMap *map, int k, uint32_t row,
                                                      uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
-      "%3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(k * 128), "r"((int)row), "r"(bar)
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
+      "%3, %4, %5}], [%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(k), "r"((int)(row >> 4)), "r"(bar)
       : "memory");
 }
 __device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -837,16 +837,17 @@ size_t tc_smem(int ntA, int ntB, int wa, int wb, int bn, int no) {
 
 }  // namespace
 
-// 2-D map of a row-major digit matrix (rows x cols bytes); a box is box_rows
-// rows (<= 256) of one 128-digit column chunk, 128-byte swizzled.
+// Map of a digit matrix (rows x cols, 16-row blocks: digit_offset) as the
+// 4-D tensor [rows/16][cols/128][16][128] bytes; a box is box_rows rows (a
+// multiple of 16, <= 256) of one 128-digit column chunk, 128-byte swizzled.
 bool tc_map_u8(void *map, const uint8_t *base, uint64_t cols, uint64_t rows, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn();
-  if (!fn || box_rows == 0 || box_rows > 256 || cols % 128) return false;
-  cuuint64_t dims[2] = {cols, rows};
-  cuuint64_t strides[1] = {cols};
-  cuuint32_t box[2] = {128, box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, (void *)base, dims, strides, box,
+  if (!fn || box_rows == 0 || box_rows > 256 || box_rows % 16 || cols % 128 || rows % 16) return false;
+  cuuint64_t dims[4] = {128, 16, cols / 128, rows / 16};
+  cuuint64_t strides[3] = {128, 2048, (cols / 128) * 2048};
+  cuuint32_t box[4] = {128, 16, 1, box_rows / 16};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 4, (void *)base, dims, strides, box,
             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -1059,23 +1060,30 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     return tcg_gemm(*c->plan1, err, s, c->out);
   }
   if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req < 0) {  // 256 x BN tiles on SM pairs
-    // Split K over up to 4 SM pairs per tile (a cluster of up to 8 CTAs) while
-    // the grid still fits one wave and every chunk keeps >= 8 stages: shapes
-    // with few output tiles and a long K then use the whole GPU.  128-column
-    // tiles are taken where 256-column ones, split, would still leave more
-    // than half of the SM pairs idle and the narrower tiles occupy more.
+    // Tile width and K split.  A split sums partials over distributed shared
+    // memory, which costs more the more chunks there are: candidates in order
+    // of preference, the first that keeps at least half the SM pairs busy in
+    // one wave wins, else the one that keeps the most busy.  (An M=256 N=128
+    // pair MMA takes as long as an N=256 one, so narrow tiles only pay where
+    // they replace a wider split.)
     const uint64_t mt = (a.M + 255) / 256;
     int bn = bn_req == kPairVariant128 ? 128 : 256;
     int splits = pair_splits(mt * ((a.N + bn - 1) / bn), a.nstages, bn);
     if (bn_req < 0) {
       const uint64_t pairs = (uint64_t)sm_count_cached() / 2;
-      const uint64_t used256 = mt * ((a.N + 255) / 256) * splits;
-      const int s128 = pair_splits(mt * ((a.N + 127) / 128), a.nstages, 128);
-      const uint64_t tiles128 = mt * ((a.N + 127) / 128);
-      const uint64_t used128 = tiles128 * s128;
-      if (2 * used256 < pairs && used128 > used256 && used128 <= pairs) {
-        bn = 128;
-        splits = s128;
+      static const int cand[6][2] = {{256, 1}, {256, 2}, {128, 1}, {128, 2}, {256, 4}, {128, 4}};
+      uint64_t best_used = 0;
+      for (const auto &cv : cand) {
+        const int cb = cv[0], cs = cv[1];
+        const uint64_t tiles = mt * ((a.N + cb - 1) / cb);
+        if (cs > 1 && (a.nstages / cs < 8 || tiles > (uint64_t)pair_max_clusters(cs, cb))) continue;
+        const uint64_t used = std::min<uint64_t>(tiles * cs, pairs);
+        if (used > best_used) {
+          best_used = used;
+          bn = cb;
+          splits = cs;
+        }
+        if (2 * used >= pairs) break;
       }
     }
     if (bn == 128 && !c->digit_map_b64_ready) {

@@ -119,7 +119,7 @@ __device__ __forceinline__ uint32_t digits4(uint32_t x, int nbits, uint4 tab) {
 }
 
 // The lane's 32 digits of padded row r (0 past nrows and past ncols) into the
-// digit matrix [nrows_a][64 * wpr] (digit_offset).
+// digit matrix (64 * wpr columns, 16-row blocks: digit_offset).
 __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int nbits, uint64_t nrows,
                                                uint64_t ncols, uint64_t wpr, uint4 tab, uint64_t r, uint64_t col0,
                                                const uint32_t (&q)[8]) {

@@ -59,12 +59,16 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
       : "memory");
 }
 
-// Rows [row, row + box) x digits [128 k, 128 k + 128) of a digit matrix
-// through its 2-D map (tc_map_u8): the box lands in shared memory as
-// box x 128 bytes, 128-byte swizzled.
+// Rows [row, row + box) (row a multiple of 16) x digits [128 k, 128 k + 128)
+// of a digit matrix through its blocked 4-D map (tc_map_u8): the box lands
+// in shared memory as box x 128 bytes, rows in order, 128-byte swizzled.
 __device__ __forceinline__ void tma_load_digits(uint32_t dst, const CUtensorMap *map, int k, uint32_t row,
                                                 uint32_t bar) {
-  tma_load_2d(dst, map, k * 128, (int)row, bar);
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(k), "r"((int)(row >> 4)), "r"(bar)
+      : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
