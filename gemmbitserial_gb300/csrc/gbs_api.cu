@@ -185,10 +185,11 @@ uint64_t gbs_debug_launch_count(void) { return g_launches.load(); }
 
 uint32_t gbs_debug_tc_error(void) { return tc_error_word(); }
 
-int gbs_debug_last_pair(const gbs_ctx *c, int *bn, int *splits) {
-  if (!c || !bn || !splits) return fail(GBS_EINVAL, "gbs_debug_last_pair: NULL argument");
+int gbs_debug_last_pair(const gbs_ctx *c, int *bn, int *splits, int *persistent) {
+  if (!c || !bn || !splits || !persistent) return fail(GBS_EINVAL, "gbs_debug_last_pair: NULL argument");
   *bn = c->last_pair_bn;
   *splits = c->last_pair_splits;
+  *persistent = c->last_pair_persistent ? 1 : 0;
   return GBS_OK;
 }
 
@@ -560,8 +561,8 @@ int gbs_clear(gbs_ctx *c, int side, void *stream) {
 int gbs_set_variant(gbs_ctx *c, int variant) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_variant: ctx is NULL");
   if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256 || variant == kPairVariant ||
-        variant == kPairVariant128))
-    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128, 256, 512 or 513");
+        variant == kPairVariant128 || variant == kPairVariantPersistent))
+    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128, 256, 512, 513 or 514");
   c->variant = variant;
   return GBS_OK;
 }

@@ -691,6 +691,156 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   }
 }
 
+// Persistent SM-pair kernel, 256 x 256 tiles, for grids of more tiles than
+// the GPU has SM pairs: each 2-CTA cluster p of P loops over tiles p, p + P,
+// ...  and accumulates its j-th tile in TMEM buffer j & 1 (2 x 256 columns),
+// so the epilogue of one tile overlaps the MMAs of the next instead of a
+// second wave repeating launch, setup and the first load.  The operand ring
+// runs on across tiles; the leader's TMA loads both CTAs' halves as in
+// gemm_tc_pair_kernel.  Barriers (same offsets in both CTAs): full / empty
+// of the ring; acc_full[2], committed (multicast) by the MMA thread when a
+// tile's accumulator is complete; acc_empty[2] in the leader, where the 4
+// epilogue warps of both CTAs (the peer's remotely) arrive once they have
+// read a buffer, before the MMAs may write it again.
+__global__ void __launch_bounds__(kPairThreads, 1)
+    gemm_tc_pair_persistent_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                                   TmaArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t peer = cluster_rank() & 1u;  // clusters of 2: rank 0 leads
+  constexpr uint16_t kPairMask = 3;
+  constexpr uint32_t stage_bytes = 2 * kPairHalfBytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.stages * stage_bytes);
+  const uint32_t full = smem_u32(bars), empty = full + 8 * a.stages, acc_full = empty + 8 * a.stages;
+  const uint32_t acc_empty = acc_full + 16, mma_done = acc_empty + 16;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * a.stages + 5);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const uint32_t npairs = gridDim.x >> 1, pid = blockIdx.x >> 1;
+  // tiles in M-fastest order (tile t = row block t % mt of column block t / mt): the pairs running at
+  // once write whole columns of the M-major result, which measured ~2.5x faster than N-fastest
+  const uint32_t mt = (uint32_t)((a.M + 255) / 256), ntiles = mt * (uint32_t)((a.N + 255) / 256), nk = a.nstages;
+
+  if (tid == 0) {
+    for (int i = 0; i < a.stages; i++) {
+      mbar_init(full + 8 * i, 1);
+      mbar_init(empty + 8 * i, 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(acc_full + 8 * b, 1);
+      mbar_init(acc_empty + 8 * b, 8);  // 4 epilogue warps x 2 CTAs
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "n"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0 && peer == 0) {  // the leader's TMA: both CTAs' halves of every stage
+      uint32_t g = 0;
+      bool stop = false;
+      for (uint32_t t = pid; t < ntiles && !stop; t += npairs) {
+        const uint32_t m0 = (t % mt) * 256u, n0 = (t / mt) * 256u;
+        for (uint32_t k = 0; k < nk; k++, g++) {
+          const uint32_t s = g % a.stages, use = g / a.stages;
+          if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) {
+            stop = true;
+            break;
+          }
+          const uint32_t fb = map_to_rank(full + 8 * s, 0);
+          mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
+          const uint32_t dst = smem_u32(smem + s * stage_bytes), pdst = map_to_rank(dst, 1);
+          tma_load_digits_pair(dst, &tmA, (int)k, m0, fb);
+          tma_load_digits_pair(dst + kPairHalfBytes, &tmB, (int)k, n0, fb);
+          tma_load_digits_pair(pdst, &tmA, (int)k, m0 + 128, fb);
+          tma_load_digits_pair(pdst + kPairHalfBytes, &tmB, (int)k, n0 + 128, fb);
+        }
+      }
+      if (*abort_flag)  // wait (bounded) for the loads the barriers still expect
+        for (uint32_t q = (g > (uint32_t)a.stages ? g - a.stages : 0); q < g; q++)
+          mbar_drain(full + 8 * (q % a.stages), (q / a.stages) & 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && peer == 0) {  // the leader issues the pair's MMAs
+      bool ok = true;
+      uint32_t g = 0, j = 0;
+      for (uint32_t t = pid; t < ntiles && ok; t += npairs, j++) {
+        const uint32_t b = j & 1u, dacc = tmem + b * 256u;
+        if (j >= 2 && !mbar_wait(acc_empty + 8 * b, ((j >> 1) - 1) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        for (uint32_t k = 0; k < nk; k++, g++) {
+          const uint32_t s = g % a.stages;
+          if (!mbar_wait(full + 8 * s, (g / a.stages) & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t base = smem_u32(smem + s * stage_bytes);
+#pragma unroll
+          for (int kk = 0; kk < 4; kk++)
+            mma_f8_pair(dacc, sw128_desc(base + kk * 32), sw128_desc(base + kPairHalfBytes + kk * 32), a.idesc,
+                        (k | kk) != 0);
+          mma_commit_pair(empty + 8 * s, kPairMask);
+        }
+        if (ok) mma_commit_pair(acc_full + 8 * b, kPairMask);
+      }
+      if (!ok) {  // issued MMAs finish before TMEM is freed
+        asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done)
+                     : "memory");
+        mbar_drain(mma_done, 0);
+      }
+    }
+  } else {  // epilogue: this CTA's 128 rows of every tile
+    const int q = warp & 3;
+    uint32_t j = 0;
+    for (uint32_t t = pid; t < ntiles; t += npairs, j++) {
+      const uint32_t b = j & 1u;
+      if (!__all_sync(0xffffffffu, mbar_wait(acc_full + 8 * b, (j >> 1) & 1, abort_flag))) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint64_t gm = (uint64_t)(t % mt) * 256u + 128u * peer + (uint32_t)(q * 32 + lane);
+      const uint64_t n0 = (uint64_t)(t / mt) * 256u;
+      const uint32_t taddr = tmem + b * 256u + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int col = 0; col < 256; col += 32) {
+        uint32_t v[32];
+        tmem_ld32(taddr + (uint32_t)col, v);
+        tmem_wait_ld(v);
+        store_cols(a, v, gm, n0 + col);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) {  // this warp is done with the buffer: tell the leader's MMA thread
+        if (peer == 0) {
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acc_empty + 8 * b) : "memory");
+        } else {
+          const uint32_t rb = map_to_rank(acc_empty + 8 * b, 0);
+          asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(rb) : "memory");
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(512));
+  }
+}
+
 // Throughput probe: one CTA per SM, one thread issuing back-to-back
 // tcgen05.mma (M=128, N=256) from fixed zeroed shared tiles; KIND 0 = e4m3
 // (K=32), KIND 1 = bf16 (K=16).  A commit + bounded wait closes every 64
@@ -1059,7 +1209,8 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     if (!err) return cudaErrorInvalidSymbol;
     return tcg_gemm(*c->plan1, err, s, c->out);
   }
-  if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req < 0) {  // 256 x BN tiles on SM pairs
+  if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req == kPairVariantPersistent || bn_req < 0) {
+    // 256 x BN tiles on SM pairs
     // Tile width and K split.  A split sums partials over distributed shared
     // memory, which costs more the more chunks there are: candidates in order
     // of preference, the first that keeps at least half the SM pairs busy in
@@ -1093,6 +1244,49 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     }
     a.splits = splits;
     a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+    // The persistent kernel (pairs looping over tiles with two TMEM
+    // accumulators) runs only when forced (variant 514, about three tiles per
+    // pair) or chosen by the tuner: past one wave it overlaps each tile's
+    // epilogue with the next tile's MMAs, but its epilogue stores measured
+    // ~2.5x slower than the same stores in gemm_tc_pair_kernel, which left
+    // it no faster than two waves of that kernel at 4096 x 2048 x 2048.
+    if (bn_req == kPairVariantPersistent) {
+      const uint64_t ntiles = mt * ((a.N + 255) / 256);
+      a.splits = 1;
+      a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+      a.stages = pair_stages(256);
+      size_t smem = 1024 + (size_t)a.stages * 2 * kPairHalfBytes + 8 * (2 * a.stages + 5) + 16;
+      while (smem > kPairSmemCap && a.stages > 2) {
+        a.stages--;
+        smem = 1024 + (size_t)a.stages * 2 * kPairHalfBytes + 8 * (2 * a.stages + 5) + 16;
+      }
+      const uint64_t npairs = std::max<uint64_t>(1, (ntiles + 2) / 3);
+      cudaError_t e = cudaFuncSetAttribute(gemm_tc_pair_persistent_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      cudaLaunchConfig_t cfg;
+      memset(&cfg, 0, sizeof(cfg));
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 2;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)(2 * npairs));
+      cfg.blockDim = dim3(kPairThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      if (!c->digit_maps_ready) return cudaErrorInvalidValue;
+      const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
+      const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_db);
+      e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_persistent_kernel, ma, mb, a);
+      count_launch();
+      c->last_pair_bn = 256;
+      c->last_pair_splits = 1;
+      c->last_pair_persistent = true;
+      return e != cudaSuccess ? e : cudaGetLastError();
+    }
     a.stages = pair_stages(bn);
     const size_t smem = pair_smem_bytes(bn);
     cudaLaunchConfig_t cfg;
@@ -1105,6 +1299,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     count_launch();
     c->last_pair_bn = bn;
     c->last_pair_splits = a.splits;
+    c->last_pair_persistent = false;
     return e != cudaSuccess ? e : cudaGetLastError();
   }
   const int bn = (bn_req == 128 || bn_req == 256) ? bn_req : (a.N > 128 ? 256 : 128);

@@ -182,6 +182,7 @@ struct gbs_ctx {
   alignas(64) unsigned char tc_map_db64[128];  // rhs digits in 64-row boxes (the pair kernel's 128-column tiles)
   bool digit_map_b64_ready = false;
   int last_pair_bn = 0, last_pair_splits = 0;  // configuration of the last SM-pair launch (test hook)
+  bool last_pair_persistent = false;
   // one-problem plan of the persistent tensor-core kernel (shapes with a side under 256 rows)
   gbs::TcgPlan *plan1 = nullptr;
   bool plan1_ready = false;
@@ -239,6 +240,7 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn);
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
 constexpr int kPairVariant = 512;     // tensor-core variant: 256 x 256 tiles on SM pairs (tcgen05 cta_group::2)
 constexpr int kPairVariant128 = 513;  // the same with 256 x 128 tiles
+constexpr int kPairVariantPersistent = 514;  // persistent SM pairs looping over 256 x 256 tiles
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 

@@ -298,6 +298,7 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
     cands[nc++] = Cand{GBS_PIPE_TC, 256};
     cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant};
     cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant128};
+    cands[nc++] = Cand{GBS_PIPE_TC, kPairVariantPersistent};
   }
   if (tc_exact(c, GBS_PIPE_TC_SMEM)) {
     cands[nc++] = Cand{GBS_PIPE_TC_SMEM, 256};

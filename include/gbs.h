@@ -189,8 +189,9 @@ GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);
  * of rhs per 128-row lhs tile on one SM), or 512 / 513 for GBS_PIPE_TC:
  * 256 x 256 / 256 x 128 tiles computed by pairs of SMs (tcgen05
  * cta_group::2), K split over up to 4 pairs of one cluster when the tiles are
- * too few to fill the GPU; -1 restores the built-in rule.  No reference
- * counterpart. */
+ * too few to fill the GPU, or 514: persistent SM pairs looping over
+ * 256 x 256 tiles (about three per pair; a tuner candidate); -1 restores the
+ * built-in rule.  No reference counterpart. */
 GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
 
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
@@ -336,9 +337,9 @@ GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 /* Number of kernel launches the library has issued since load (all entry points). */
 GBS_API uint64_t gbs_debug_launch_count(void);
 
-/* Tile width (256 or 128) and K split (1, 2 or 4) of the last SM-pair kernel
- * launched for ctx; both 0 if none was. */
-GBS_API int gbs_debug_last_pair(const gbs_ctx *ctx, int *bn, int *splits);
+/* Tile width (256 or 128), K split (1, 2 or 4) and whether the persistent
+ * kernel ran (1) for the last SM-pair launch of ctx; all 0 if none was. */
+GBS_API int gbs_debug_last_pair(const gbs_ctx *ctx, int *bn, int *splits, int *persistent);
 
 #ifdef __cplusplus
 }

@@ -172,10 +172,10 @@ def test_tc_digit_cache_follows_reimport():
         deallocGEMMContext(ctx)
 
 
-def last_pair(ctx):
-    bn, sp = C.c_int(0), C.c_int(0)
-    _capi.check(_capi.load().gbs_debug_last_pair(ctx._h, C.byref(bn), C.byref(sp)))
-    return bn.value, sp.value
+def last_pair(ctx, with_persistent=False):
+    bn, sp, pe = C.c_int(0), C.c_int(0), C.c_int(0)
+    _capi.check(_capi.load().gbs_debug_last_pair(ctx._h, C.byref(bn), C.byref(sp), C.byref(pe)))
+    return (bn.value, sp.value, pe.value) if with_persistent else (bn.value, sp.value)
 
 
 # (variant, M, K, N, expected K split): 1, 2 and 4 pairs per tile at both tile widths
@@ -223,5 +223,52 @@ def test_pair_auto_fills_the_gpu_for_few_tiles():
         assert sha(ctx.res.reshape(N, M)) == CFG["gemm_256x9216x4096_bpbp"]["sha256"]
         bn, sp = last_pair(ctx)
         assert bn in (128, 256) and sp >= 2 and (N // bn) * sp * 2 >= pairs, (bn, sp, pairs)
+    finally:
+        deallocGEMMContext(ctx)
+
+
+PERSIST_CASES = [(512, 1024, 768), (300, 700, 600), (1024, 512, 1024), (257, 2048, 513)]
+
+
+@pytest.mark.parametrize("shape", PERSIST_CASES, ids=[f"{m}x{k}x{n}" for (m, k, n) in PERSIST_CASES])
+def test_pair_persistent(shape):
+    """Persistent SM pairs (variant 514: ~3 tiles per pair, so both TMEM accumulators are reused)."""
+    M, K, N = shape
+    rng = np.random.default_rng(M + 3 * K + 5 * N)
+    for (wa, ea, wb, eb) in [(3, "u", 2, "s"), (1, "b", 1, "b"), (4, "s", 1, "u"), (2, "s", 3, "u")]:
+        A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+        B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+        sa, sb = ea != "u", eb != "u"
+        ctx = allocGEMMContext(M, K, N, wa, wb, sa, sb)
+        try:
+            _capi.check(_capi.load().gbs_set_variant(ctx._h, 514))
+            ctx.set_pipe(_capi.GBS_PIPE_TC)
+            ctx.lhs.importRegular(A)
+            ctx.rhs.importRegular(B)
+            gemmBitSerial(ctx)
+            got = ctx.res.reshape(N, M).copy()
+            assert last_pair(ctx, True) == (256, 1, 1)
+            gemmBitSerial(ctx)  # a second launch over the same context
+            assert np.array_equal(ctx.res.reshape(N, M), got)
+        finally:
+            deallocGEMMContext(ctx)
+        assert np.array_equal(got, O.oracle_gemm(A, B, wa, wb, sa, sb)), (shape, wa, ea, wb, eb)
+    assert _capi.load().gbs_debug_tc_error() == 0
+
+
+def test_pair_persistent_full_size():
+    """4096 x 2048 x 2048 (128 tiles of 256 x 256, past one wave) on the persistent kernel: the
+    reference's result bits."""
+    name = "gemm_4096x2048x2048_u2bp"
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+    ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    try:
+        _capi.check(_capi.load().gbs_set_variant(ctx._h, 514))
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        gemmBitSerial(ctx)
+        assert sha(ctx.res.reshape(N, M)) == CFG[name]["sha256"]
+        assert last_pair(ctx, True) == (256, 1, 1)
     finally:
         deallocGEMMContext(ctx)
