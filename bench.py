@@ -1,6 +1,7 @@
 """Benchmark of the bit-serial GEMM hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+                    [--pipe auto|popc|bmma|tc|tc_pairs|tc_smem] [--variant V] [--no-configs ...]
 
 A step is one gemmBitSerial over one pair of packed operands: by default the
 2048 x 4096 x 2048 GEMM of a 3-bit unsigned lhs with a 2-bit signed rhs.  The
@@ -41,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "bit-exact GOPS @2048x4096x2048 w3/w2; grouped & adjoint speedup vs plain GPU"
+PIPE_CHOICES = {"auto": 0, "popc": 1, "bmma": 2, "tc": 3, "tc_pairs": 4, "tc_smem": 5}  # GBS_PIPE_*
 DEFAULT_WORKLOAD = "gemm_2048x4096x2048_u3s2"
 
 
@@ -56,6 +58,10 @@ def parse():
     p.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-problem measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
     p.add_argument("--no-configs", action="store_true", help="skip the per-config forward measurements")
+    p.add_argument("--pipe", default="auto", choices=sorted(PIPE_CHOICES),
+                   help="force the forward pipe of the headline workload (default: the library's choice)")
+    p.add_argument("--variant", type=int, default=-1,
+                   help="force the pipe variant (gbs_set_variant) of the headline workload")
     return p.parse_args()
 
 
@@ -469,8 +475,15 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    def force(c):  # --pipe / --variant: the same choice for the resident and the end-to-end context
+        if args.pipe != "auto":
+            c.set_pipe(PIPE_CHOICES[args.pipe])
+        if args.variant != -1:
+            _capi.check(lib.gbs_set_variant(c._h, args.variant))
+
     # ---- resident path: packed operands in HBM
     ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    force(ctx)
     dA = torch.from_numpy(A).to(dev)
     dB = torch.from_numpy(B).to(dev)
     with torch.cuda.stream(stream):
@@ -512,6 +525,7 @@ def run_ours(args):
     hB = torch.from_numpy(B).pin_memory()
     hR = torch.empty(M * N, dtype=torch.int32).pin_memory()
     ctx2 = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    force(ctx2)
 
     def e2e_step():
         _capi.check(lib.gbs_import(ctx2._h, 0, C.c_void_p(hA.data_ptr()), _capi.GBS_I8, 0, sh))
@@ -539,8 +553,12 @@ def run_ours(args):
     if pipe in (_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS, _capi.GBS_PIPE_TC_SMEM):
         f8, bf16 = C.c_double(), C.c_double()
         _capi.check(lib.gbs_tc_peaks(C.byref(f8), C.byref(bf16)))
-        if pipe == _capi.GBS_PIPE_TC:  # the built-in rule of the digit pipe (no variant forced)
-            kernel = "gemm_tc_pair_kernel" if (M >= 256 and N >= 256) else "gemm_tcg_kernel"
+        if pipe == _capi.GBS_PIPE_TC and args.variant in (128, 256):
+            kernel = "gemm_tc_tma_kernel"
+        elif pipe == _capi.GBS_PIPE_TC and args.variant == 514:
+            kernel = "gemm_tc_pair_persistent_kernel"
+        elif pipe == _capi.GBS_PIPE_TC:  # the built-in rule of the digit pipe, or a forced SM-pair variant
+            kernel = "gemm_tc_pair_kernel" if (M >= 256 and N >= 256) or args.variant in (512, 513) else "gemm_tcg_kernel"
         else:
             kernel = "gemm_tc_kernel"
         digits = pipe != _capi.GBS_PIPE_TC_PAIRS
@@ -558,7 +576,7 @@ def run_ours(args):
     else:
         popc, bmma = C.c_double(), C.c_double()
         _capi.check(lib.gbs_pipe_peaks(C.byref(popc), C.byref(bmma)))
-        kernel = "gemm_popc_tiled"
+        kernel = "gemm_bmma_kernel" if pipe == _capi.GBS_PIPE_BMMA else "gemm_popc_tiled"
         binops = 2.0 * M * N * kpad * wA * wB  # AND + add per bit of each plane pair
         achieved = binops / (ms * 1e-3) / 1e12
         peak = 2.0 * popc.value / 1e12
@@ -590,7 +608,9 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded splitmix64)",
             "config": dict(desc, parallelism=f"replicas x{world}", l2="flushed before every step (256 MiB write, outside the timed events)",
                            pipe={1: "popc", 2: "bmma", 3: "tcgen05 (HBM digits, TMA)", 4: "tcgen05 (smem plane pairs)",
-                                 5: "tcgen05 (smem digits)"}.get(pipe, str(pipe))),
+                                 5: "tcgen05 (smem digits)"}.get(pipe, str(pipe)),
+                           **({"forced": {"pipe": args.pipe, "variant": args.variant}}
+                              if args.pipe != "auto" or args.variant != -1 else {})),
             "parity": parity,
             "e2e": {"value": round(replica_gops(M, K, N, e2e_s, world), 3), "unit": "GOPS",
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),
