@@ -74,7 +74,7 @@ bool is_device_ptr(const void *p) {
 }
 
 // Address through which this device reads or writes caller memory `p`, or
-// nullptr when it cannot: device and managed memory as they are, pinned host
+// nullptr when it cannot: its own and managed memory as they are, pinned host
 // memory through its mapped device address, and (with `pageable`) pageable
 // host memory as it is where the GPU walks the host's page tables
 // (NVLink-C2C systems such as GB300).  GBS_HOST_DIRECT=0 turns the host cases
@@ -87,7 +87,8 @@ void *device_view(const void *p, int dev, bool pageable_ok) {
     cudaGetLastError();
     return nullptr;
   }
-  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void *>(p);
+  if (a.type == cudaMemoryTypeManaged) return const_cast<void *>(p);
+  if (a.type == cudaMemoryTypeDevice) return a.device == dev ? const_cast<void *>(p) : nullptr;  // other GPUs: copies
   if (!host_direct) return nullptr;
   if (a.type == cudaMemoryTypeHost) return a.devicePointer;
   static int pageable[64];  // 0 unknown, 1 yes, 2 no

@@ -82,7 +82,9 @@ typedef struct {
 typedef struct {
   gbs_matrix_info lhs, rhs;
   uint64_t lhsBlock, rhsBlock; /* device tile rows (lhs, rhs) */
-  int32_t *res;                /* DEVICE pointer, rhs.nrows x lhs.nrows, transposed layout */
+  int32_t *res;                /* DEVICE pointer, rhs.nrows x lhs.nrows, transposed layout: the
+                                  last gbs_gemm's result (not written by gbs_gemm_to into a caller
+                                  buffer) */
   int pipe;                    /* pipe the next gbs_gemm will use */
 } gbs_ctx_info;
 
