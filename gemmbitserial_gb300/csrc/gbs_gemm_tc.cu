@@ -492,12 +492,19 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
                : "memory");
 }
 // 32 columns n0 .. n0+31 of result row m: res[n*M + m], lanes on consecutive m.
+// One base pointer and a fixed column stride; whole 32-column blocks store
+// without per-column predicates.
 __device__ __forceinline__ void store_cols(const TmaArgs &a, const uint32_t (&v)[32], uint64_t gm, uint64_t n0) {
   if (gm >= a.M) return;
+  const uint64_t M = a.M;
+  int32_t *p = a.C + n0 * M + gm;
+  if (n0 + 32 <= a.N) {
 #pragma unroll
-  for (int j = 0; j < 32; j++) {
-    const uint64_t gn = n0 + j;
-    if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
+    for (int j = 0; j < 32; j++) p[(uint64_t)j * M] = __float2int_rn(__uint_as_float(v[j]));
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+      if (n0 + j < a.N) p[(uint64_t)j * M] = __float2int_rn(__uint_as_float(v[j]));
   }
 }
 
@@ -1244,14 +1251,14 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     }
     a.splits = splits;
     a.idesc = (1u << 4) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
-    // The persistent kernel (pairs looping over tiles with two TMEM
-    // accumulators) runs only when forced (variant 514, about three tiles per
-    // pair) or chosen by the tuner: past one wave it overlaps each tile's
-    // epilogue with the next tile's MMAs, but its epilogue stores measured
-    // ~2.5x slower than the same stores in gemm_tc_pair_kernel, which left
-    // it no faster than two waves of that kernel at 4096 x 2048 x 2048.
-    if (bn_req == kPairVariantPersistent) {
-      const uint64_t ntiles = mt * ((a.N + 255) / 256);
+    // More 256 x 256 tiles than one wave holds: the persistent kernel, whose
+    // pairs loop over tiles with two TMEM accumulators, so each tile's
+    // epilogue overlaps the next tile's MMAs instead of a second wave
+    // repeating launch, setup and the first load (variant 514 forces it, with
+    // about three tiles per pair)
+    const uint64_t ntiles = mt * ((a.N + 255) / 256);
+    const uint64_t fit = (uint64_t)std::max(1, pair_max_clusters(1, 256));
+    if (bn_req == kPairVariantPersistent || (bn_req < 0 && bn == 256 && splits == 1 && ntiles > fit)) {
       a.splits = 1;
       a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
       a.stages = pair_stages(256);
@@ -1260,7 +1267,8 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
         a.stages--;
         smem = 1024 + (size_t)a.stages * 2 * kPairHalfBytes + 8 * (2 * a.stages + 5) + 16;
       }
-      const uint64_t npairs = std::max<uint64_t>(1, (ntiles + 2) / 3);
+      const uint64_t npairs =
+          bn_req == kPairVariantPersistent ? std::max<uint64_t>(1, (ntiles + 2) / 3) : std::min(ntiles, fit);
       cudaError_t e = cudaFuncSetAttribute(gemm_tc_pair_persistent_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;

@@ -192,7 +192,8 @@ GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);
  * 256 x 256 / 256 x 128 tiles computed by pairs of SMs (tcgen05
  * cta_group::2), K split over up to 4 pairs of one cluster when the tiles are
  * too few to fill the GPU, or 514: persistent SM pairs looping over
- * 256 x 256 tiles (about three per pair; a tuner candidate); -1 restores the
+ * 256 x 256 tiles (about three per pair when forced; the built-in rule takes
+ * them for grids of more tiles than one wave holds); -1 restores the
  * built-in rule.  No reference counterpart. */
 GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
 

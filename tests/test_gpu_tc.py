@@ -272,3 +272,20 @@ def test_pair_persistent_full_size():
         assert last_pair(ctx, True) == (256, 1, 1)
     finally:
         deallocGEMMContext(ctx)
+
+
+def test_pair_auto_goes_persistent_past_one_wave():
+    """4096 x 2048 x 2048 has 128 tiles of 256 x 256, more than one wave: the built-in rule runs the
+    persistent kernel, bit-exact."""
+    name = "gemm_4096x2048x2048_u2bp"
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+    ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    try:
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        gemmBitSerial(ctx)
+        assert sha(ctx.res.reshape(N, M)) == CFG[name]["sha256"]
+        assert last_pair(ctx, True) == (256, 1, 1)
+    finally:
+        deallocGEMMContext(ctx)
