@@ -262,13 +262,10 @@ __global__ void __launch_bounds__(kThreads, 1)
               "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (gm < a.M) {
+        int32_t o[32];
 #pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const uint64_t gn = n0 + col + j;
-            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
-          }
-        }
+        for (int j = 0; j < 32; j++) o[j] = __float2int_rn(__uint_as_float(v[j]));
+        store_result_cols<32>(a.C, a.M, a.N, gm, n0 + col, o);
       }
     }
   }
@@ -389,13 +386,10 @@ __global__ void __launch_bounds__(kTmaThreads, 1)
               "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (gm < a.M) {
+        int32_t o[32];
 #pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const uint64_t gn = n0 + col + j;
-            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(__uint_as_float(v[j]));
-          }
-        }
+        for (int j = 0; j < 32; j++) o[j] = __float2int_rn(__uint_as_float(v[j]));
+        store_result_cols<32>(a.C, a.M, a.N, gm, n0 + col, o);
       }
     }
   }
@@ -491,21 +485,12 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
                :
                : "memory");
 }
-// 32 columns n0 .. n0+31 of result row m: res[n*M + m], lanes on consecutive m.
-// One base pointer and a fixed column stride; whole 32-column blocks store
-// without per-column predicates.
+// 32 columns n0 .. n0+31 of result row m from fp32 accumulator bits.
 __device__ __forceinline__ void store_cols(const TmaArgs &a, const uint32_t (&v)[32], uint64_t gm, uint64_t n0) {
-  if (gm >= a.M) return;
-  const uint64_t M = a.M;
-  int32_t *p = a.C + n0 * M + gm;
-  if (n0 + 32 <= a.N) {
+  int32_t o[32];
 #pragma unroll
-    for (int j = 0; j < 32; j++) p[(uint64_t)j * M] = __float2int_rn(__uint_as_float(v[j]));
-  } else {
-#pragma unroll
-    for (int j = 0; j < 32; j++)
-      if (n0 + j < a.N) p[(uint64_t)j * M] = __float2int_rn(__uint_as_float(v[j]));
-  }
+  for (int j = 0; j < 32; j++) o[j] = __float2int_rn(__uint_as_float(v[j]));
+  store_result_cols<32>(a.C, a.M, a.N, gm, n0, o);
 }
 
 template <int SPLITS, int BN>
@@ -675,19 +660,18 @@ __global__ void __launch_bounds__(kPairThreads, 1)
         uint32_t v[32];
         tmem_ld32(taddr + cb, v);
         tmem_wait_ld(v);
-        if (gm < a.M) {
+        int32_t o[32];
 #pragma unroll
-          for (int i = 0; i < 32; i++) {
-            float acc = __uint_as_float(v[i]);
+        for (int i = 0; i < 32; i++) {
+          float acc = __uint_as_float(v[i]);
 #pragma unroll
-            for (int qq = 0; qq < SPLITS - 1; qq++) {
-              const float4 r4 = raw[qq][i >> 2];
-              acc += (i & 3) == 0 ? r4.x : (i & 3) == 1 ? r4.y : (i & 3) == 2 ? r4.z : r4.w;
-            }
-            const uint64_t gn = n0 + c0 + cb + i;
-            if (gn < a.N) a.C[gn * a.M + gm] = __float2int_rn(acc);
+          for (int qq = 0; qq < SPLITS - 1; qq++) {
+            const float4 r4 = raw[qq][i >> 2];
+            acc += (i & 3) == 0 ? r4.x : (i & 3) == 1 ? r4.y : (i & 3) == 2 ? r4.z : r4.w;
           }
+          o[i] = __float2int_rn(acc);
         }
+        store_result_cols<32>(a.C, a.M, a.N, gm, n0 + c0 + cb, o);
       }
     }
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");

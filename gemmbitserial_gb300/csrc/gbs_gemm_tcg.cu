@@ -199,11 +199,7 @@ __global__ void __launch_bounds__(kTgThreads, 1)
         for (int i = 0; i < 16; i++) o[i] = __float2int_rn(__uint_as_float(v[i]));
         const uint32_t c0 = tl.c * P.bn + col;
         if (!P.swap) {  // row = m, column = n: lanes write 32 consecutive m of one n
-          if (row < P.M) {
-#pragma unroll
-            for (int i = 0; i < 16; i++)
-              if (c0 + i < P.N) P.C[(uint64_t)(c0 + i) * P.M + row] = o[i];
-          }
+          store_result_cols<16>(P.C, P.M, P.N, row, c0, o);
         } else if (row < P.N) {  // row = n, column = m: each lane writes a run of its result row
           int32_t *dst = P.C + (uint64_t)row * P.M + c0;
           if ((P.M & 3u) == 0) {
