@@ -518,6 +518,8 @@ def run_ours(args):
     got = hashlib.sha256(np.ascontiguousarray(res).tobytes()).hexdigest()
     parity = "bit-exact vs reference (sha256)" if got == want else ("MISMATCH" if want else "unchecked")
     pipe = ctx.pipe
+    last_pair = [C.c_int(0), C.c_int(0), C.c_int(0)]  # tile width, K split, persistent of the last pair launch
+    _capi.check(lib.gbs_debug_last_pair(ctx._h, *(C.byref(x) for x in last_pair)))
     deallocGEMMContext(ctx)
 
     # ---- end to end through the C ABI from pinned host buffers
@@ -557,8 +559,9 @@ def run_ours(args):
             kernel = "gemm_tc_tma_kernel"
         elif pipe == _capi.GBS_PIPE_TC and args.variant == 514:
             kernel = "gemm_tc_pair_persistent_kernel"
-        elif pipe == _capi.GBS_PIPE_TC:  # the built-in rule of the digit pipe, or a forced SM-pair variant
-            kernel = "gemm_tc_pair_kernel" if (M >= 256 and N >= 256) or args.variant in (512, 513) else "gemm_tcg_kernel"
+        elif pipe == _capi.GBS_PIPE_TC:  # the kernel the library's rule (or a forced variant) launched
+            bn, pe = last_pair[0].value, last_pair[2].value
+            kernel = ("gemm_tc_pair_persistent_kernel" if pe else "gemm_tc_pair_kernel") if bn else "gemm_tcg_kernel"
         else:
             kernel = "gemm_tc_kernel"
         digits = pipe != _capi.GBS_PIPE_TC_PAIRS
