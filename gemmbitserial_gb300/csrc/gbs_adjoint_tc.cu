@@ -174,11 +174,20 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
 #pragma unroll
         for (int j = 0; j < 32; j++) sc[lane * 33 + j] = __uint_as_float(hi[j]) + __uint_as_float(lo[j]);
         __syncwarp();
-        const uint32_t col = k0 + c + lane;
+        // rows r0 + 32q .. +31 of this column block: one base pointer, a fixed
+        // row stride, no per-element predicate when all 32 rows exist
+        const uint32_t col = k0 + c + lane, row0 = r0 + q * 32;
+        if (col < a.K) {
+          float *p = a.out + (uint64_t)row0 * a.K + col;
+          const uint64_t K = a.K;
+          if (row0 + 32 <= a.R) {
+#pragma unroll 8
+            for (int i = 0; i < 32; i++) p[(uint64_t)i * K] = sc[i * 33 + lane];
+          } else {
 #pragma unroll 4
-        for (int i = 0; i < 32; i++) {
-          const uint32_t row = r0 + q * 32 + i;
-          if (row < a.R && col < a.K) a.out[(uint64_t)row * a.K + col] = sc[i * 33 + lane];
+            for (int i = 0; i < 32; i++)
+              if (row0 + i < a.R) p[(uint64_t)i * K] = sc[i * 33 + lane];
+          }
         }
         __syncwarp();
       }
