@@ -23,13 +23,13 @@
 // [N][M] (dB: r = n, s = m) and transposed as [M][N] (dA: r = m, s = n), and
 // the operand values transposed as Vt[k][s] in bf16.
 //
-// GEMM kernel: CTA tile 128 rows (r) x 256 columns (k), 64 values of s per
-// stage: TMA loads the three 128 x 64 split tiles and the 256 x 64 value tile
-// (128-byte swizzle), warp 1 issues 12 tcgen05.mma.kind::f16 (M=128, N=256,
-// K=16) per stage into the two accumulators (all 512 TMEM columns), warps
-// 2-5 add the accumulators and store through a padded shared-memory tile so
-// that each warp store covers 128 contiguous bytes of a row of Out.  Every
-// mbarrier wait is bounded.
+// GEMM kernel: CTA tile 128 rows (r) x 256 columns (k), 32 values of s per
+// stage in a 5-stage ring: TMA loads the three 128 x 32 split tiles and the
+// 256 x 32 value tile (64-byte swizzle), warp 1 issues 6 tcgen05.mma.kind::f16
+// (M=128, N=256, K=16) per stage into the two accumulators (all 512 TMEM
+// columns), warps 2-5 add the accumulators and store through a padded
+// shared-memory tile so that each warp store covers 128 contiguous bytes of a
+// row of Out.  Every mbarrier wait is bounded.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -42,16 +42,23 @@
 namespace gbs {
 namespace {
 
-constexpr int kAdjStages = 2;
-constexpr uint32_t kAdjSplitBytes = 128 * 128;          // 128 rows x 64 bf16
-constexpr uint32_t kAdjValBytes = 256 * 128;            // 256 rows x 64 bf16
-constexpr uint32_t kAdjStageBytes = 3 * kAdjSplitBytes + kAdjValBytes;
 constexpr int kAdjThreads = 192;
 constexpr uint32_t kAdjScratchFloats = 32 * 33;          // per epilogue warp
+
+// Ring: 32 values of s per stage (64-byte rows, 64-byte swizzle), 5 stages of
+// 40 KB.  Two stages of 64 values (80 KB, 128-byte rows) hold the same bytes
+// but free them half as often; that ring ran the GEMMs latency-bound, 15 %
+// slower per adjoint.
+constexpr int kAdjKs = 32;
+constexpr int kAdjStages = 5;
+constexpr uint32_t kAdjSplitBytes = 128 * kAdjKs * 2;  // 128 rows x 32 bf16
+constexpr uint32_t kAdjValBytes = 256 * kAdjKs * 2;    // 256 rows x 32 bf16
+constexpr uint32_t kAdjStageBytes = 3 * kAdjSplitBytes + kAdjValBytes;
 
 constexpr size_t adj_smem_bytes() {
   return 1024 + kAdjStages * kAdjStageBytes + 4 * kAdjScratchFloats * 4 + 8 * (2 * kAdjStages + 2) + 16;
 }
+static_assert(adj_smem_bytes() <= 232448, "shared memory per CTA");
 
 struct AdjTcArgs {
   float *out;  // R x K row-major
@@ -120,7 +127,7 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         if (use > 0 && !mbar_wait_err(empty + 8 * s, (use - 1) & 1, abort_flag, err)) break;
         mbar_expect_tx(full + 8 * s, kAdjStageBytes);
         const uint32_t dst = smem_u32(smem + s * kAdjStageBytes);
-        const int x = (int)(k * 64);
+        const int x = (int)(k * kAdjKs);
         tma_load_2d(dst, &tmHi, x, (int)r0, full + 8 * s);
         tma_load_2d(dst + kAdjSplitBytes, &tmMid, x, (int)r0, full + 8 * s);
         tma_load_2d(dst + 2 * kAdjSplitBytes, &tmLo, x, (int)r0, full + 8 * s);
@@ -143,12 +150,12 @@ __global__ void __launch_bounds__(kAdjThreads, 1)
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t base = smem_u32(smem + s * kAdjStageBytes), vb = base + 3 * kAdjSplitBytes;
 #pragma unroll
-        for (int kk = 0; kk < 4; kk++) {
-          const uint64_t bd = sw128_desc(vb + kk * 32);
+        for (int kk = 0; kk < kAdjKs / 16; kk++) {  // K = 16 per MMA: 32 bytes along the row
+          const uint64_t bd = sw64_desc(vb + kk * 32);
           const uint32_t first = (k | kk) != 0;
-          mma_bf16(tmem, sw128_desc(base + kk * 32), bd, a.idesc, first);
-          mma_bf16(tmem + 256, sw128_desc(base + kAdjSplitBytes + kk * 32), bd, a.idesc, first);
-          mma_bf16(tmem + 256, sw128_desc(base + 2 * kAdjSplitBytes + kk * 32), bd, a.idesc, 1u);
+          mma_bf16(tmem, sw64_desc(base + kk * 32), bd, a.idesc, first);
+          mma_bf16(tmem + 256, sw64_desc(base + kAdjSplitBytes + kk * 32), bd, a.idesc, first);
+          mma_bf16(tmem + 256, sw64_desc(base + 2 * kAdjSplitBytes + kk * 32), bd, a.idesc, 1u);
         }
         mma_commit(empty + 8 * s);
       }
@@ -358,16 +365,17 @@ EncodeTiledFn adj_encode_fn() {
   return fn;
 }
 
-// 2-D bf16 map over [rows][cols] (row pitch `pitch` elements), box 64 x box_rows, 128-byte swizzle.
+// 2-D bf16 map over [rows][cols] (row pitch `pitch` elements), box 32 x box_rows
+// (64-byte rows), 64-byte swizzle.
 bool bf16_map(CUtensorMap *map, const void *base, uint64_t cols, uint64_t rows, uint64_t pitch, uint32_t box_rows) {
   EncodeTiledFn fn = adj_encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {pitch * 2};
-  cuuint32_t box[2] = {64, box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)kAdjKs, box_rows};
   cuuint32_t estr[2] = {1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)base, dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -467,7 +475,7 @@ cudaError_t launch_gemm(const CUtensorMap (&split)[3], const CUtensorMap &vmap, 
   a.out = out;
   a.R = (uint32_t)R;
   a.K = (uint32_t)K;
-  a.nstages = (uint32_t)((S + 63) / 64);
+  a.nstages = (uint32_t)((S + kAdjKs - 1) / kAdjKs);
   // kind::f16: D fp32, A and B bf16, both K-major, M = 128, N = 256
   a.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
   uint32_t *err = tc_error_ptr();
