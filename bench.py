@@ -576,6 +576,9 @@ def run_ours(args):
                 "work": "2*M*N*K fp8 FLOPs (digit mode: all plane pairs in one MMA)" if digits
                         else "2*M*N*K*wA*wB fp8 plane-pair FLOPs",
                 "bf16_peak_measured": round(bf16.value / 1e12, 1)}
+        if kernel.startswith("gemm_tc_pair"):  # the tile and K split the library chose (or was forced to)
+            roof["pair_tile"] = f"256x{last_pair[0].value}"
+            roof["k_split"] = last_pair[1].value
     else:
         popc, bmma = C.c_double(), C.c_double()
         _capi.check(lib.gbs_pipe_peaks(C.byref(popc), C.byref(bmma)))
