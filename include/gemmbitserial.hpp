@@ -57,7 +57,12 @@ class BitSerialMatrix {
     (void)colalign;
     gbs_ctx *c = nullptr;
     detail::check(gbs_ctx_alloc(nrows, ncols, 0, nbits, 1, issigned ? 1 : 0, 0, &c));
-    return from_ctx(c, GBS_LHS);
+    try {
+      return from_ctx(c, GBS_LHS);
+    } catch (...) {
+      gbs_ctx_free(c);
+      throw;
+    }
   }
 
   // BitSerialMatrix::dealloc (reference gemmbitserial.hpp:38-40) for matrices made by alloc().
@@ -200,13 +205,18 @@ inline GEMMContext allocGEMMContext(uint64_t lhsRows, uint64_t depth, uint64_t r
   detail::check(gbs_ctx_alloc(lhsRows, depth, rhsRows, lhsBits, rhsBits, lhsSigned ? 1 : 0, rhsSigned ? 1 : 0, &c));
   GEMMContext g;
   g.handle = c;
-  g.lhs = BitSerialMatrix::from_ctx(c, GBS_LHS);
-  g.rhs = BitSerialMatrix::from_ctx(c, GBS_RHS);
-  gbs_ctx_info info;
-  detail::check(gbs_ctx_get_info(c, &info));
-  g.lhsBlock = info.lhsBlock;
-  g.rhsBlock = info.rhsBlock;
-  g.res = new int32_t[lhsRows * rhsRows + 1]();  // zeroed: its pages exist before the device writes them
+  try {  // the context is freed if anything below throws
+    g.lhs = BitSerialMatrix::from_ctx(c, GBS_LHS);
+    g.rhs = BitSerialMatrix::from_ctx(c, GBS_RHS);
+    gbs_ctx_info info;
+    detail::check(gbs_ctx_get_info(c, &info));
+    g.lhsBlock = info.lhsBlock;
+    g.rhsBlock = info.rhsBlock;
+    g.res = new int32_t[lhsRows * rhsRows + 1]();  // zeroed: its pages exist before the device writes them
+  } catch (...) {
+    gbs_ctx_free(c);
+    throw;
+  }
   return g;
 }
 
