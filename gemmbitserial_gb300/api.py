@@ -62,6 +62,20 @@ def _src(arr, allow_float: bool = False):
     return C.c_void_p(a.ctypes.data), _NP2DT[a.dtype], a
 
 
+def _release(keep, source, stream) -> None:
+    """Drops a contiguous copy _src made of a device tensor.  The import may still
+    read it on `stream`; torch reuses a freed block in the order of the stream it
+    was allocated on (the current one), so for another stream wait first."""
+    if stream is None or keep is source:
+        return
+    try:
+        import torch
+    except ImportError:
+        return
+    if isinstance(keep, torch.Tensor) and keep.is_cuda:
+        torch.cuda.synchronize(keep.device)
+
+
 class BitSerialMatrix:
     """One operand of a context (gemmbitserial.hpp:19-50); the planes live on the GPU."""
 
@@ -111,7 +125,7 @@ class BitSerialMatrix:
         ptr, dt, keep = _src(matrix, allow_float=True)
         _capi.check(_capi.load().gbs_import(self._ctx._h, self._side, ptr, dt, int(bool(readColMajor)),
                                             _stream_handle(stream)))
-        del keep
+        _release(keep, matrix, stream)
 
     def importRegularAndQuantize(self, matrix, thresholds, nThres=None, readColMajor: bool = False,
                                  stream=None) -> None:
@@ -128,7 +142,9 @@ class BitSerialMatrix:
             tptr, tkeep = None, None
         _capi.check(_capi.load().gbs_import_quantize(self._ctx._h, self._side, ptr, tptr, int(nThres), dt,
                                                      int(bool(readColMajor)), _stream_handle(stream)))
-        del keep, tkeep
+        _release(keep, matrix, stream)
+        if tkeep is not None:
+            _release(tkeep, thresholds, stream)
 
     # single bits (gemmbitserial.hpp:90-108); each call synchronises the device
     def get(self, bit: int, row: int, col: int) -> bool:
