@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 
@@ -352,17 +353,20 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeTiledFn adj_encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
+  static std::atomic<EncodeTiledFn> fn{nullptr};  // racing first calls store the same value
+  EncodeTiledFn f = fn.load(std::memory_order_relaxed);
+  if (!f) {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-    else
+        q == cudaDriverEntryPointSuccess) {
+      f = (EncodeTiledFn)p;
+      fn.store(f, std::memory_order_relaxed);
+    } else {
       cudaGetLastError();
+    }
   }
-  return fn;
+  return f;
 }
 
 // 2-D bf16 map over [rows][cols] (row pitch `pitch` elements), box 32 x box_rows

@@ -91,17 +91,19 @@ void *device_view(const void *p, int dev, bool pageable_ok) {
   if (a.type == cudaMemoryTypeDevice) return a.device == dev ? const_cast<void *>(p) : nullptr;  // other GPUs: copies
   if (!host_direct) return nullptr;
   if (a.type == cudaMemoryTypeHost) return a.devicePointer;
-  static int pageable[64];  // 0 unknown, 1 yes, 2 no
+  static std::atomic<int> pageable[64];  // 0 unknown, 1 yes, 2 no (racing first calls store the same value)
   if (!pageable_ok || dev < 0 || dev >= 64) return nullptr;
-  if (!pageable[dev]) {
+  int known = pageable[dev].load(std::memory_order_relaxed);
+  if (!known) {
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
       cudaGetLastError();
       v = 0;
     }
-    pageable[dev] = v ? 1 : 2;
+    known = v ? 1 : 2;
+    pageable[dev].store(known, std::memory_order_relaxed);
   }
-  return pageable[dev] == 1 ? const_cast<void *>(p) : nullptr;
+  return known == 1 ? const_cast<void *>(p) : nullptr;
 }
 
 size_t elem_size(int dtype) { return dtype == GBS_I16 ? 2 : (dtype == GBS_I32 || dtype == GBS_F32) ? 4 : 1; }

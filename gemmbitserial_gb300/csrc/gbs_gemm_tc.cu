@@ -28,6 +28,7 @@
 // stops issuing work, waits (bounded) for what it issued and frees TMEM.
 #include <cuda.h>
 
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -936,18 +937,23 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// The process-wide lookups below are idempotent: threads that race on a
+// first call store the same value, so relaxed atomics suffice.
 EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
+  static std::atomic<EncodeTiledFn> fn{nullptr};
+  EncodeTiledFn f = fn.load(std::memory_order_relaxed);
+  if (!f) {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-    else
+        q == cudaDriverEntryPointSuccess) {
+      f = (EncodeTiledFn)p;
+      fn.store(f, std::memory_order_relaxed);
+    } else {
       cudaGetLastError();
+    }
   }
-  return fn;
+  return f;
 }
 
 // Tensor map over all planes of one operand: 2-D u64 [nbits * nrows_a][wpr], box 128 rows x 2 words.
@@ -1083,15 +1089,17 @@ cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
 namespace {
 
 int sm_count_cached() {
-  static int cache[64] = {};
+  static std::atomic<int> cache[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
-  if (!cache[dev]) {
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (!n) {
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) cudaGetLastError();
-    cache[dev] = v > 0 ? v : 1;
+    n = v > 0 ? v : 1;
+    cache[dev].store(n, std::memory_order_relaxed);
   }
-  return cache[dev];
+  return n;
 }
 
 // Stages of the pair kernel's ring for BN-column tiles, and its shared memory.
@@ -1139,10 +1147,11 @@ void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1],
 // Clusters of 2 * splits CTAs that fit the GPU at once (they are placed within
 // one GPC each), cached per device.
 int pair_max_clusters(int splits, int bn) {
-  static int cache[64][5][2] = {};
+  static std::atomic<int> cache[64][5][2];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-  int &v = cache[dev][splits][bn == 128 ? 1 : 0];
+  std::atomic<int> &slot = cache[dev][splits][bn == 128 ? 1 : 0];
+  int v = slot.load(std::memory_order_relaxed);
   if (v == 0) {
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
@@ -1155,6 +1164,7 @@ int pair_max_clusters(int splits, int bn) {
       n = 0;
     }
     v = n > 0 ? n : -1;
+    slot.store(v, std::memory_order_relaxed);
   }
   return v > 0 ? v : 0;
 }
@@ -1373,18 +1383,20 @@ int tc_peaks(double *f8, double *bf16) {
 }
 
 uint32_t *tc_error_ptr() {
-  static uint32_t *addr[64] = {};
+  static std::atomic<uint32_t *> addr[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!addr[dev]) {
+  uint32_t *a = addr[dev].load(std::memory_order_relaxed);
+  if (!a) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_tc_error) != cudaSuccess) {
       cudaGetLastError();
       return nullptr;
     }
-    addr[dev] = static_cast<uint32_t *>(p);
+    a = static_cast<uint32_t *>(p);
+    addr[dev].store(a, std::memory_order_relaxed);
   }
-  return addr[dev];
+  return a;
 }
 
 uint32_t tc_error_word() {
