@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default=DEFAULT_WORKLOAD)
-    p.add_argument("--cpu-seconds", type=float, default=8.0, help="budget of the CPU baseline sample")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample (seconds)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-grouped", action="store_true", help="skip the grouped 512-problem measurement")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint measurement")
