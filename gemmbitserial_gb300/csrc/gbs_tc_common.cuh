@@ -112,10 +112,6 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                : "memory");
 }
 
-// 4 bits -> 4 bytes holding 0 or 1 (bit i -> byte i); the multiply places the
-// bits at 0..3, 7..10, 14..17, 21..24 without carries, the mask keeps 0, 8, 16, 24.
-__device__ __forceinline__ uint32_t spread4(uint32_t nib) { return (nib * 0x00204081u) & 0x01010101u; }
-
 __device__ __forceinline__ uint32_t bfe4(uint32_t x, int sh) {
   uint32_t r;
   asm("bfe.u32 %0, %1, %2, 4;" : "=r"(r) : "r"(x), "r"(sh));
