@@ -228,7 +228,7 @@ extern "C" int gbs_adjoint(gbs_ctx *c, const float *dC, float *dA, float *dB, vo
   if (!c) return fail(GBS_EINVAL, "gbs_adjoint: ctx is NULL");
   if (!c->lhs.imported || !c->rhs.imported) return fail(GBS_ESTATE, "gbs_adjoint: import both operands first");
   const uint64_t M = c->lhs.nrows, N = c->rhs.nrows;
-  if ((dA || dB) && M * N && !dC) return fail(GBS_EINVAL, "gbs_adjoint: dC is NULL");
+  if ((dA || dB) && M && N && !dC) return fail(GBS_EINVAL, "gbs_adjoint: dC is NULL");
   for (const void *p : {(const void *)dC, (const void *)dA, (const void *)dB}) {
     if (!p) continue;
     cudaPointerAttributes at;

@@ -501,8 +501,8 @@ int adjoint_tc(gbs_ctx *c, const float *dC, float *dA, float *dB, cudaStream_t s
   if (M * K + N * K == 0) return GBS_OK;
   if (M == 0 || N == 0) {  // an empty contraction: zero gradients
     cudaError_t e = cudaSuccess;
-    if (dA && M * K) e = cudaMemsetAsync(dA, 0, M * K * 4, s);
-    if (e == cudaSuccess && dB && N * K) e = cudaMemsetAsync(dB, 0, N * K * 4, s);
+    if (dA && M && K) e = cudaMemsetAsync(dA, 0, M * K * 4, s);
+    if (e == cudaSuccess && dB && N && K) e = cudaMemsetAsync(dB, 0, N * K * 4, s);
     return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_adjoint: memset");
   }
   if (!c->adj) {

@@ -702,7 +702,7 @@ int gbs_get_planes(gbs_ctx *c, int side, uint64_t *dst, void *stream) {
   return GBS_OK;
 }
 
-static int to_dst(gbs_ctx *c, int32_t *dst, uint64_t n, cudaStream_t s,
+static int to_dst(int32_t *dst, uint64_t n, cudaStream_t s,
                   cudaError_t (*fill)(const Mat &, int32_t *, cudaStream_t), const Mat &m, const char *who) {
   if (n == 0) return GBS_OK;
   if (!dst) return fail(GBS_EINVAL, std::string(who) + ": dst is NULL");
@@ -727,7 +727,7 @@ int gbs_sum_rows(gbs_ctx *c, int side, int32_t *dst, void *stream) {
   if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_sum_rows: bad side");
   DeviceGuard g(c->device);
   const Mat &m = side ? c->rhs : c->lhs;
-  return to_dst(c, dst, m.nrows, as_stream(stream), launch_rowsum, m, "gbs_sum_rows");
+  return to_dst(dst, m.nrows, as_stream(stream), launch_rowsum, m, "gbs_sum_rows");
 }
 
 int gbs_export(gbs_ctx *c, int side, int32_t *dst, void *stream) {
@@ -735,7 +735,7 @@ int gbs_export(gbs_ctx *c, int side, int32_t *dst, void *stream) {
   if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_export: bad side");
   DeviceGuard g(c->device);
   const Mat &m = side ? c->rhs : c->lhs;
-  return to_dst(c, dst, m.nrows * m.ncols, as_stream(stream), launch_export, m, "gbs_export");
+  return to_dst(dst, m.nrows * m.ncols, as_stream(stream), launch_export, m, "gbs_export");
 }
 
 }  // extern "C"

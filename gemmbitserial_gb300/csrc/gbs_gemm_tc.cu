@@ -1132,7 +1132,7 @@ void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1],
   with_pair_kernel(splits, bn, [&](auto kern) {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   });
-  memset(&cfg, 0, sizeof(cfg));
+  cfg = cudaLaunchConfig_t{};
   cfg.blockDim = dim3(kPairThreads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
@@ -1267,7 +1267,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       cudaLaunchConfig_t cfg;
-      memset(&cfg, 0, sizeof(cfg));
+      cfg = cudaLaunchConfig_t{};
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
       attr[0].val.clusterDim.x = 2;

@@ -99,7 +99,7 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
       if (dt < GBS_I8 || dt > GBS_F32) return fail(GBS_EINVAL, "gbs_group: unknown dtype");
       const Mat &m = side ? g->ctxs[p]->rhs : g->ctxs[p]->lhs;
       if (m.nrows_a == 0 || m.wpr() == 0) continue;
-      if (m.nrows * m.ncols && (!src || !device_ptr(src)))
+      if (m.nrows && m.ncols && (!src || !device_ptr(src)))
         return fail(GBS_EINVAL, "gbs_group: sources must be device pointers (problem " + std::to_string(p) + ")");
       PackJob j;
       memset(&j, 0, sizeof(j));
