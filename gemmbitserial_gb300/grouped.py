@@ -10,7 +10,7 @@ from __future__ import annotations
 import ctypes as C
 
 from . import _capi
-from .api import GEMMContext, _stream_handle
+from .api import _stream_handle
 
 _DT = None
 

@@ -1,6 +1,5 @@
 """Autotuner store: versioned text file, save/load round trip, entries from
 another version ignored.  No GPU needed."""
-import pytest
 
 
 def test_store_roundtrip_and_version_check(gbs_lib, tmp_path):
