@@ -231,6 +231,8 @@ extern "C" int gbs_adjoint(gbs_ctx *c, const float *dC, float *dA, float *dB, vo
   if ((dA || dB) && M && N && !dC) return fail(GBS_EINVAL, "gbs_adjoint: dC is NULL");
   for (const void *p : {(const void *)dC, (const void *)dA, (const void *)dB}) {
     if (!p) continue;
+    // the kernels move rows of 4 floats as 16-byte vectors
+    if ((uintptr_t)p % 16 != 0) return fail(GBS_EINVAL, "gbs_adjoint: dC, dA and dB must be 16-byte aligned");
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess ||
         (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {

@@ -230,7 +230,8 @@ GBS_API uint64_t gbs_noalloc_scratch_bytes(void);
  *   dA[m*K + k] = sum_n dC[n*M + m] * B[n,k]     (M x K, row-major)
  *   dB[n*K + k] = sum_m dC[n*M + m] * A[m,k]     (N x K, the rhs layout)
  * with A, B the values the planes encode (bipolar: +-1; signed MSB negative).
- * FP32 accumulation.  dC, dA, dB are DEVICE pointers; dA or dB may be NULL to
+ * FP32 accumulation.  dC, dA, dB are DEVICE pointers, 16-byte aligned (as
+ * cudaMalloc returns them; GBS_EINVAL otherwise); dA or dB may be NULL to
  * skip that gradient.  Asynchronous on `stream`. */
 GBS_API int gbs_adjoint(gbs_ctx *ctx, const float *dC, float *dA, float *dB, void *stream);
 

@@ -162,6 +162,29 @@ def test_adjoint_rejects_host_pointers(lib):
     deallocGEMMContext(ctx)
 
 
+def test_adjoint_rejects_misaligned_pointers(lib):
+    """dC, dA and dB must be 16-byte aligned (the kernels move 4 floats at a time): a pointer 4 bytes
+    into a device buffer is refused on the host.  The outputs that would be written stay NULL or
+    aligned-to-4 views, so even a missing check could not launch a misaligned vector access."""
+    import torch
+    M, K, N = 64, 128, 32
+    A = datagen.operand(datagen.SEED_BASE + 90, M, K, 2, "u")
+    B = datagen.operand(datagen.SEED_BASE + 91, N, K, 1, "b")
+    ctx = allocGEMMContext(M, K, N, 2, 1, False, True)
+    try:
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        d = torch.zeros(N * M + 4, dtype=torch.float32, device="cuda")
+        out = torch.zeros(M * K + 4, dtype=torch.float32, device="cuda")
+        rc = lib.gbs_adjoint(ctx._h, C.c_void_p(d.data_ptr() + 4), None, None, None)
+        assert rc == _capi.GBS_EINVAL and b"aligned" in _capi.load().gbs_last_error()
+        rc = lib.gbs_adjoint(ctx._h, C.c_void_p(d.data_ptr()), C.c_void_p(out.data_ptr() + 4), None, None)
+        assert rc == _capi.GBS_EINVAL
+        torch.cuda.synchronize()
+    finally:
+        deallocGEMMContext(ctx)
+
+
 def test_adjoint_cache_follows_reimport(adjoint_pipe):
     """The tensor-core adjoint caches its transposed operand values; a new import replaces them."""
     import torch
