@@ -42,7 +42,7 @@ enum {
   GBS_ECUDA = 3,       /* a CUDA runtime call failed */
   GBS_ESTATE = 4,      /* call out of order (e.g. gemm before both imports) */
   GBS_ETIMEOUT = 5,    /* a bounded device wait gave up */
-  GBS_EUNSUPPORTED = 6 /* valid request this build does not implement */
+  GBS_EUNSUPPORTED = 6 /* valid request the library or the device cannot serve */
 };
 
 /* Element types accepted by gbs_import.  GBS_I8/I16/I32 follow the

@@ -1,7 +1,7 @@
 /*
  * gbs_oracle.c -- CPU oracle for the bit-serial GEMM path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the tests, the smoke
  * entry and the CPU-baseline leg of the benchmark call it to produce the
  * results the GPU path must reproduce bit for bit.  Nothing in the product
  * library links against it or falls back to it.

@@ -1,7 +1,7 @@
 """Python access to the CPU oracle (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module.  It is the checker the GPU path is compared
+``bench.py`` import this module.  It is the oracle the GPU path is compared
 against, never part of the product path.
 
 * ``liboracle.so`` (built from ``gbs_oracle.c``) restates the reference's
