@@ -432,7 +432,7 @@ def measure_adjoint(lib, dev, stream, reps=10, warmup=3):
 
 
 def measured_peaks() -> dict:
-    """The machine's measured peaks (HBM copy GB/s, cuBLAS bf16 TF/s burst and sustained), if present."""
+    """Measured peaks of this GPU type (HBM copy GB/s, cuBLAS bf16 TF/s burst and sustained), if present."""
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return json.load(f)
@@ -441,7 +441,7 @@ def measured_peaks() -> dict:
 
 
 def adjoint_roofline(achieved: float, mma_rate: float) -> dict:
-    """The bf16 adjoint kernel against the machine's measured bf16 peak (cuBLAS burst: the kernel is
+    """The bf16 adjoint kernel against the measured bf16 peak of this GPU type (cuBLAS burst: the kernel is
     timed alone), with this process's raw MMA-loop rate beside it."""
     mp = measured_peaks()
     peak, src = mp.get("bf16_tflops"), "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 GEMM, burst)"

@@ -1,5 +1,5 @@
-"""bench.py's adjoint roofline on the host: the measured bf16 peak of the pool when its
-file is present, the fallback figure when it is not."""
+"""bench.py's adjoint roofline on the host: the measured bf16 peak when its file is
+present, the fallback figure when it is not."""
 import json
 import os
 import sys
