@@ -49,13 +49,16 @@ int scratch_address(int dev, uint64_t **out) {
   return GBS_OK;
 }
 
-bool on_device(const void *p) {
+// True when the kernels launched on device `dev` may address `p` directly:
+// managed memory, or device memory of `dev` itself.  Another GPU's memory is
+// refused (reading it without peer access faults), and so is host memory.
+bool on_device(const void *p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
 }
 
 uint64_t round_up(uint64_t x, uint64_t a) { return (x + a - 1) / a * a; }
@@ -96,11 +99,11 @@ extern "C" int gbs_gemm_noalloc(const void *lhs, int lhs_dtype, const void *rhs,
     return fail(GBS_EINVAL, "gbs_gemm_noalloc: this GEMM needs " + std::to_string(need_words * 8) +
                                 " bytes of scratch; the fixed array holds " + std::to_string(kScratchWords * 8));
   if ((K && (!lhs || !rhs)) || !res) return fail(GBS_EINVAL, "gbs_gemm_noalloc: NULL pointer");
-  if ((K && (!on_device(lhs) || !on_device(rhs))) || !on_device(res))
-    return fail(GBS_EINVAL, "gbs_gemm_noalloc: inputs and result must be device pointers");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_gemm_noalloc: cudaGetDevice");
+  if ((K && (!on_device(lhs, dev) || !on_device(rhs, dev))) || !on_device(res, dev))
+    return fail(GBS_EINVAL, "gbs_gemm_noalloc: inputs and result must be memory of the current device");
   uint64_t *scratch = nullptr;
   int rc = scratch_address(dev, &scratch);
   if (rc != GBS_OK) return rc;

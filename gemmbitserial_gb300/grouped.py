@@ -12,8 +12,6 @@ import ctypes as C
 from . import _capi
 from .api import _stream_handle
 
-_DT = None
-
 
 def _dtype_code(t):
     import torch

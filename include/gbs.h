@@ -208,7 +208,9 @@ GBS_API int gbs_set_pipe(gbs_ctx *ctx, int pipe);
  * gemmBitSerial of device inputs straight into a device result:
  *   res[n*M + m] = sum_k A[m*K + k] * B[n*K + k]   (bit-exact, int32 wrap)
  * with lhs = A (M x K) and rhs = B (N x K) row-major DEVICE arrays of the
- * given GBS_* element types, encoded as in gbs_import.  It allocates nothing:
+ * given GBS_* element types, encoded as in gbs_import.  Inputs and result
+ * must be memory of the current device (or managed memory); another GPU's
+ * memory or host memory is rejected with GBS_EINVAL.  It allocates nothing:
  * the packed planes and row sums live in one fixed file-scope device array of
  * gbs_noalloc_scratch_bytes() bytes (16 MiB), which every GPU that loads the
  * library holds until exit.  A GEMM whose packed operands do not fit is

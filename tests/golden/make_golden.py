@@ -3,8 +3,7 @@
 Run where the reference sources exist (it reads them; the fixtures it writes
 travel with the repository):
 
-    make -C oracle ref                # compiles the unmodified reference
-    python tests/golden/make_golden.py [REFDIR]
+    python tests/golden/make_golden.py REFDIR   # compiles the unmodified reference from REFDIR first
 
 Writes
   mnist_kat.npz   -- the reference's known-answer test (test/mnistdata.h,
@@ -226,7 +225,10 @@ def make_config_hashes() -> None:
 
 
 if __name__ == "__main__":
-    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFDIR", "/root/reference")
+    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFDIR")
+    if not refdir or not os.path.isfile(os.path.join(refdir, "gemmbitserial.hpp")):
+        sys.exit("usage: make_golden.py REFDIR   (or REFDIR=... in the environment): the reference checkout")
+    os.environ["REFDIR"] = refdir  # the oracle Makefile builds the reference from there
     if not O.ref_available():
         O.build(ref=True)
     make_mnist(refdir)

@@ -26,3 +26,20 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": "GOPS", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    assert cb["one_core"]["cores"] == 1 and cb["one_core"]["value"] > 0
+    # the same config dict as the GPU arm's line (bench_config), so the two lines compare as one workload
+    sys.path.insert(0, ROOT)
+    import bench
+    M, K, N = 8, 8192, 8
+    assert line["config"] == bench.bench_config(bench.workload_desc("gemm_8x8192x8_u1u1"), M, K, N, 1, 1)
+
+
+def test_resident_contexts_exceed_twice_the_l2():
+    sys.path.insert(0, ROOT)
+    import bench
+    for (M, K, N, wA, wB) in [(2048, 4096, 2048, 3, 2), (256, 9216, 4096, 1, 4), (8, 8192, 8, 1, 1),
+                              (4096, 2048, 2048, 2, 1)]:
+        P = bench.resident_contexts(M, K, N, wA, wB)
+        per = (M + N) * K * (1 + max(wA, wB) / 8.0) + 4.0 * M * N
+        assert 2 <= P <= 16
+        assert P == 16 or P * per >= 2 * bench.L2_BYTES

@@ -24,3 +24,12 @@ def test_adjoint_roofline_falls_back_without_measured_peaks(monkeypatch, tmp_pat
     r = bench.adjoint_roofline(950.0, 0.0)
     assert r["peak"] == 1900.0 and r["frac"] == 0.5 and "fallback" in r["peak_source"]
     assert r["frac_of_mma_loop_rate"] is None
+
+
+def test_adjoint_roofline_reports_the_algorithmic_fp32_fraction(monkeypatch, tmp_path):
+    (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"bf16_tflops": 2000.0}))
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    r = bench.adjoint_roofline(1200.0, 2400.0, 400.0)
+    assert r["frac"] == 0.6 and r["frac_of_mma_loop_rate"] == 0.5
+    assert r["algorithmic_fp32"]["achieved"] == 400.0
+    assert r["algorithmic_fp32"]["frac"] == 0.2 and r["algorithmic_fp32"]["frac_of_mma_loop_rate"] == round(400 / 2400, 4)
