@@ -62,6 +62,8 @@ def parse():
                    help="force the forward pipe of the headline workload (default: the library's choice)")
     p.add_argument("--variant", type=int, default=-1,
                    help="force the pipe variant (gbs_set_variant) of the headline workload")
+    p.add_argument("--no-tuner", action="store_true",
+                   help="ignore the committed tuner store (the library's built-in rule picks every kernel)")
     return p.parse_args()
 
 
@@ -70,6 +72,41 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return world, rank, local
+
+
+TUNER_STORE = os.path.join(ROOT, "gemmbitserial_gb300", "tuned", "gb300_sm103a.txt")
+
+
+def load_tuner(lib, args):
+    """Loads the committed GB300 tuner store (written by gemmbitserial_gb300.tune_workloads) unless
+    --no-tuner or GBS_TUNER_STORE names another; returns the path in use or None."""
+    from gemmbitserial_gb300 import _capi
+    if args.no_tuner:
+        _capi.check(lib.gbs_tuner_clear())
+        return None
+    if os.environ.get("GBS_TUNER_STORE"):
+        return os.environ["GBS_TUNER_STORE"]
+    if not os.path.exists(TUNER_STORE):
+        return None
+    _capi.check(lib.gbs_tuner_load(TUNER_STORE.encode(), 1))
+    return os.path.relpath(TUNER_STORE, ROOT)
+
+
+def tuner_entry(lib, ctx):
+    """The tuner store's entry a context's AUTO choice follows, or None."""
+    pipe, variant, us = C.c_int(), C.c_int(), C.c_double()
+    if lib.gbs_tuner_lookup(ctx._h, C.byref(pipe), C.byref(variant), C.byref(us)) != 0:
+        return None
+    return {"pipe": {1: "popc", 2: "bmma", 3: "tc", 4: "tc_pairs", 5: "tc_smem"}.get(pipe.value, pipe.value),
+            "variant": variant.value, "tuned_us": round(us.value, 2)}
+
+
+def pair_kernel_name(last_pair):
+    """The SM-pair kernel a context's last launch ran (gbs_debug_last_pair), or None if none did."""
+    bn, _, kind = (x.value for x in last_pair)
+    if not bn:
+        return None
+    return {0: "gemm_tc_pair_kernel", 1: "gemm_tc_pair_persistent_kernel", 2: "gemm_tc_pair_streamk_kernel"}[kind]
 
 
 def workload_desc(name):
@@ -359,12 +396,16 @@ def measure_configs(lib, dev, stream, reps=50, warmup=5):
         res = ctx.res.reshape(N, M)
         ok = hashlib.sha256(np.ascontiguousarray(res).tobytes()).hexdigest() == gold.get(name, {}).get("sha256")
         pipe = ctx.pipe
+        tuned = tuner_entry(lib, ctx)
+        lp = [C.c_int(0), C.c_int(0), C.c_int(0)]
+        _capi.check(lib.gbs_debug_last_pair(ctx._h, *(C.byref(x) for x in lp)))
         deallocGEMMContext(ctx)
         kpad = (K + 63) // 64 * 64
         packed = wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N
         out[name] = {"ms": round(ms, 4), "gops": round(gops(M, K, N, ms * 1e-3), 1), "pipe": names.get(pipe, pipe),
                      "tbinops": round(2.0 * M * N * kpad * wA * wB / (ms * 1e-3) / 1e12, 2),
                      "gbs_packed_bytes": round(packed / (ms * 1e-3) / 1e9, 1),
+                     "tuned": tuned, "pair_kernel": pair_kernel_name(lp),
                      "parity": "bit-exact vs reference (sha256)" if ok else "MISMATCH"}
     return out
 
@@ -501,6 +542,7 @@ def run_ours(args):
     from gemmbitserial_gb300 import _capi, datagen
     from gemmbitserial_gb300.api import allocGEMMContext, deallocGEMMContext
     lib = _capi.load()
+    tuner_store = load_tuner(lib, args)
     M, K, N, wA, sA, wB, sB, A, B = datagen.workload(args.workload)
     desc = workload_desc(args.workload)
     stream = torch.cuda.Stream(device=dev)
@@ -568,7 +610,8 @@ def run_ours(args):
     parity = ("bit-exact vs reference (sha256, every context)" if got == {want} else
               ("MISMATCH" if want else "unchecked"))
     pipe = ctxs[0].pipe
-    last_pair = [C.c_int(0), C.c_int(0), C.c_int(0)]  # tile width, K split, persistent of the last pair launch
+    tuned = tuner_entry(lib, ctxs[0])
+    last_pair = [C.c_int(0), C.c_int(0), C.c_int(0)]  # tile width, K split / pairs, kernel kind of the last pair launch
     _capi.check(lib.gbs_debug_last_pair(ctxs[0]._h, *(C.byref(x) for x in last_pair)))
     for ctx in ctxs:
         deallocGEMMContext(ctx)
@@ -606,13 +649,11 @@ def run_ours(args):
     if pipe in (_capi.GBS_PIPE_TC, _capi.GBS_PIPE_TC_PAIRS, _capi.GBS_PIPE_TC_SMEM):
         f8, bf16 = C.c_double(), C.c_double()
         _capi.check(lib.gbs_tc_peaks(C.byref(f8), C.byref(bf16)))
-        if pipe == _capi.GBS_PIPE_TC and args.variant in (128, 256):
+        if pipe == _capi.GBS_PIPE_TC and (args.variant in (128, 256) or
+                                          (args.variant == -1 and tuned and tuned["variant"] in (128, 256))):
             kernel = "gemm_tc_tma_kernel"
-        elif pipe == _capi.GBS_PIPE_TC and args.variant == 514:
-            kernel = "gemm_tc_pair_persistent_kernel"
-        elif pipe == _capi.GBS_PIPE_TC:  # the kernel the library's rule (or a forced variant) launched
-            bn, pe = last_pair[0].value, last_pair[2].value
-            kernel = ("gemm_tc_pair_persistent_kernel" if pe else "gemm_tc_pair_kernel") if bn else "gemm_tcg_kernel"
+        elif pipe == _capi.GBS_PIPE_TC:  # the kernel the library's rule, the tuner or a forced variant launched
+            kernel = pair_kernel_name(last_pair) or "gemm_tcg_kernel"
         else:
             kernel = "gemm_tc_kernel"
         digits = pipe != _capi.GBS_PIPE_TC_PAIRS
@@ -627,9 +668,12 @@ def run_ours(args):
                 "work": "2*M*N*K fp8 FLOPs (digit mode: all plane pairs in one MMA)" if digits
                         else "2*M*N*K*wA*wB fp8 plane-pair FLOPs",
                 "bf16_peak_measured": round(bf16.value / 1e12, 1)}
-        if kernel.startswith("gemm_tc_pair"):  # the tile and K split the library chose (or was forced to)
+        if kernel in ("gemm_tc_pair_kernel", "gemm_tc_pair_persistent_kernel"):  # the tile and K split that ran
             roof["pair_tile"] = f"256x{last_pair[0].value}"
             roof["k_split"] = last_pair[1].value
+        elif kernel == "gemm_tc_pair_streamk_kernel":
+            roof["pair_tile"] = "256x256"
+            roof["sm_pairs"] = last_pair[1].value
     else:
         popc, bmma = C.c_double(), C.c_double()
         _capi.check(lib.gbs_pipe_peaks(C.byref(popc), C.byref(bmma)))
@@ -642,6 +686,7 @@ def run_ours(args):
                 "peak_source": "measured in-process (gbs_pipe_peaks: CUDA-core AND+POPC loop)",
                 "bmma_peak": round(2.0 * bmma.value / 1e12, 3)}
     roof["traffic"] = read_traffic(kernel, args.workload)
+    roof["tuner"] = {"store": tuner_store, "entry": tuned}
     roof["algorithmic_bytes"] = int(wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N)
     clocks = clk.summary()
 

@@ -68,6 +68,7 @@ SIGNATURES = {
     "gbs_tuner_load": (i32, [C.c_char_p, i32]),
     "gbs_tuner_entries": (i32, []),
     "gbs_tuner_clear": (i32, []),
+    "gbs_tuner_lookup": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_double)]),
     "gbs_last_error": (C.c_char_p, []),
     "gbs_version": (C.c_char_p, []),
     "gbs_debug_fail_alloc_after": (None, [i32]),

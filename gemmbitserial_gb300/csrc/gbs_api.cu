@@ -126,6 +126,8 @@ void free_ctx_buffers(gbs_ctx *c) {
     delete c->plan1;
   }
   adj_plan_free(c->adj);
+  if (c->sk_ws) cudaFree(c->sk_ws);
+  if (c->sk_flags) cudaFree(c->sk_flags);
   if (c->digits[0]) cudaFree(c->digits[0]);
   if (c->digits[1]) cudaFree(c->digits[1]);
 }
@@ -191,8 +193,8 @@ uint32_t gbs_debug_tc_error(void) { return tc_error_word(); }
 int gbs_debug_last_pair(const gbs_ctx *c, int *bn, int *splits, int *persistent) {
   if (!c || !bn || !splits || !persistent) return fail(GBS_EINVAL, "gbs_debug_last_pair: NULL argument");
   *bn = c->last_pair_bn;
-  *splits = c->last_pair_splits;
-  *persistent = c->last_pair_persistent ? 1 : 0;
+  *splits = c->last_pair_streamk ? c->last_pair_streamk : c->last_pair_splits;
+  *persistent = c->last_pair_streamk ? 2 : (c->last_pair_persistent ? 1 : 0);
   return GBS_OK;
 }
 
@@ -564,8 +566,10 @@ int gbs_clear(gbs_ctx *c, int side, void *stream) {
 int gbs_set_variant(gbs_ctx *c, int variant) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_variant: ctx is NULL");
   if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256 || variant == kPairVariant ||
-        variant == kPairVariant128 || variant == kPairVariantPersistent))
-    return fail(GBS_EINVAL, "gbs_set_variant: variant must be -1, 0..2, 128, 256, 512, 513 or 514");
+        variant == kPairVariant128 || variant == kPairVariantPersistent || variant == kPairVariantStreamK ||
+        pair_split_variant(variant)))
+    return fail(GBS_EINVAL,
+                "gbs_set_variant: variant must be -1, 0..2, 128, 256, 512..515, 1281, 1282, 1284, 2561, 2562 or 2564");
   c->variant = variant;
   return GBS_OK;
 }

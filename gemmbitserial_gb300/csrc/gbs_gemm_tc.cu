@@ -441,6 +441,14 @@ __device__ __forceinline__ void tma_load_digits_pair(uint32_t dst, const CUtenso
       "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(0), "r"(k), "r"((int)(row >> 4)), "r"(bar)
       : "memory");
 }
+// L2 prefetch of the box tma_load_digits(_pair) would load (a hint: no data
+// lands in shared memory and no barrier is signalled).
+__device__ __forceinline__ void tma_prefetch_digits(const CUtensorMap *map, int k, uint32_t row) {
+  asm volatile("cp.async.bulk.prefetch.tensor.4d.L2.global.tile [%0, {%1, %2, %3, %4}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(0), "r"(0), "r"(k), "r"((int)(row >> 4))
+               : "memory");
+}
 __device__ __forceinline__ void mma_f8_pair(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                             uint32_t acc) {
   asm volatile(
@@ -486,6 +494,19 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&v)[32]) {
                :
                : "memory");
 }
+// Marks registers a TMEM load filled as produced after the tcgen05.wait::ld
+// issued just before (volatile asm keeps its place in program order): for
+// several loads in flight behind one wait.
+__device__ __forceinline__ void tmem_after_wait(uint32_t (&v)[32]) {
+  asm volatile(""
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                 "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15]),
+                 "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]), "+r"(v[22]),
+                 "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]), "+r"(v[29]),
+                 "+r"(v[30]), "+r"(v[31])
+               :
+               : "memory");
+}
 // 32 columns n0 .. n0+31 of result row m from fp32 accumulator bits.
 __device__ __forceinline__ void store_cols(const TmaArgs &a, const uint32_t (&v)[32], uint64_t gm, uint64_t n0) {
   int32_t o[32];
@@ -516,6 +537,25 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   const uint32_t k_lo = split * a.nstages / SPLITS, k_hi = (split + 1) * a.nstages / SPLITS;
   const uint32_t nk = k_hi - k_lo;
   bool tile_done = false;  // epilogue warps: the accumulator is complete
+  griddep_launch_dependents();
+  if (tid == 0) {  // descriptors towards the TMA unit before the first load needs them
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+  }
+  if (tid == 64 && peer == 0) {
+    // an epilogue thread (idle until the accumulator is done) sends the first
+    // three stages towards L2 while setup runs and the previous kernel
+    // finishes: about 50 ns per hint, within the setup's own time (issued
+    // from the setup thread for the whole ring, they held up its barrier
+    // initialisation by 1-2 us)
+    const uint32_t pre = nk < 3u ? nk : 3u;
+    for (uint32_t k = 0; k < pre; k++) {
+      tma_prefetch_digits(&tmA, (int)(k_lo + k), (uint32_t)pair_m0);
+      tma_prefetch_digits(&tmA, (int)(k_lo + k), (uint32_t)(pair_m0 + 128));
+      tma_prefetch_digits(&tmB, (int)(k_lo + k), (uint32_t)n0);
+      tma_prefetch_digits(&tmB, (int)(k_lo + k), (uint32_t)(n0 + BN / 2));
+    }
+  }
 
   if (tid == 0) {
     for (int i = 0; i < a.stages; i++) {
@@ -538,6 +578,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
+  griddep_wait();  // operands and result belong to the previous kernels until here
 
   if (warp == 0) {
     // The leader's TMA loads the stage for both CTAs: its own halves, and the
@@ -601,14 +642,19 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       const uint64_t gm = m0 + q * 32 + lane;
       const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16);
       if (SPLITS == 1) {
-        // one 32-column TMEM load at a time (measured faster than keeping the
-        // next load in flight during the stores)
+        // four 32-column TMEM loads behind one wait: tcgen05.wait::ld waits
+        // for all of a thread's loads, so the latency is paid once per 128
+        // columns
 #pragma unroll 1
-        for (int col = 0; col < BN; col += 32) {
-          uint32_t v[32];
-          tmem_ld32(taddr + (uint32_t)col, v);
-          tmem_wait_ld(v);
-          store_cols(a, v, gm, n0 + col);
+        for (int col = 0; col < BN; col += 128) {
+          uint32_t v[4][32];
+#pragma unroll
+          for (int i = 0; i < 4; i++) tmem_ld32(taddr + (uint32_t)(col + 32 * i), v[i]);
+          tmem_wait_ld(v[0]);
+#pragma unroll
+          for (int i = 1; i < 4; i++) tmem_after_wait(v[i]);
+#pragma unroll
+          for (int i = 0; i < 4; i++) store_cols(a, v[i], gm, n0 + col + 32 * i);
         }
       } else {
         // the columns the other K chunks reduce go into the drained ring as
@@ -712,6 +758,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   // tiles in M-fastest order (tile t = row block t % mt of column block t / mt): the pairs running at
   // once write whole columns of the M-major result, which measured ~2.5x faster than N-fastest
   const uint32_t mt = (uint32_t)((a.M + 255) / 256), ntiles = mt * (uint32_t)((a.N + 255) / 256), nk = a.nstages;
+  griddep_launch_dependents();
 
   if (tid == 0) {
     for (int i = 0; i < a.stages; i++) {
@@ -736,6 +783,7 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
+  griddep_wait();  // operands and result belong to the previous kernels until here
 
   if (warp == 0) {
     if (lane == 0 && peer == 0) {  // the leader's TMA: both CTAs' halves of every stage
@@ -806,11 +854,15 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       const uint64_t n0 = (uint64_t)(t / mt) * 256u;
       const uint32_t taddr = tmem + b * 256u + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int col = 0; col < 256; col += 32) {
-        uint32_t v[32];
-        tmem_ld32(taddr + (uint32_t)col, v);
-        tmem_wait_ld(v);
-        store_cols(a, v, gm, n0 + col);
+      for (int col = 0; col < 256; col += 128) {  // four TMEM loads behind one wait
+        uint32_t v[4][32];
+#pragma unroll
+        for (int i = 0; i < 4; i++) tmem_ld32(taddr + (uint32_t)(col + 32 * i), v[i]);
+        tmem_wait_ld(v[0]);
+#pragma unroll
+        for (int i = 1; i < 4; i++) tmem_after_wait(v[i]);
+#pragma unroll
+        for (int i = 0; i < 4; i++) store_cols(a, v[i], gm, n0 + col + 32 * i);
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       __syncwarp();
@@ -822,6 +874,256 @@ __global__ void __launch_bounds__(kPairThreads, 1)
           asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(rb) : "memory");
         }
       }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(512));
+  }
+}
+
+// ---------------------------------------------------------------- stream-K SM pairs
+// Stream-K pair kernel: the (256 x 256 tile, 128-digit K stage) units of the
+// whole GEMM are split evenly over P SM pairs (2-CTA clusters), so all pairs
+// run the same number of stages whatever the tile count.  Pair p owns units
+// [p U / P, (p+1) U / P), tiles M-fastest, and walks them from the top down
+// in segments of one tile each; segment j accumulates in TMEM buffer j & 1 so
+// its epilogue overlaps the next segment's MMAs.  A tile split over pairs is
+// finished by the pair holding its last stage (the tail): with the descending
+// walk that is the tile's last segment in time, while every other share of it
+// is the first segment of a lower pair, done early and stored as an fp32
+// partial in that pair's workspace slot.  The tail's epilogue waits
+// (bounded) for those partials' flags -- only ever on lower pairs, which
+// were dispatched first and wait on nobody before publishing -- and adds them
+// (integers below 2^24: exact).  Flags carry the launch's epoch, so the
+// workspace needs no reset.  Loads, MMAs and the TMEM buffers' handshakes are
+// those of gemm_tc_pair_persistent_kernel.  Measured on 2048 x 4096 x 2048
+// (64 tiles): over all 76 pairs it ran 28 us against 21 us for one tile per
+// pair -- a split tile's partial store, flag and reload cost more than the
+// five stages the even split saves -- so the built-in rule does not take it;
+// it is a tuner candidate (variant 515).
+struct SkArgs {
+  int32_t *C;
+  float *ws;        // [pairs][256 columns][256 rows] fp32 partial tiles
+  uint32_t *flags;  // [pairs][2 CTAs][4 warps]: epoch once that warp's partial rows are stored
+  uint64_t M, N;
+  uint32_t nk;      // K stages per tile
+  uint32_t mt;      // 256-row tiles along M
+  uint32_t units;   // tiles * nk
+  uint32_t epoch;
+  uint32_t idesc;
+  int stages;
+};
+
+struct SkSeg {
+  uint32_t t, k0, k1;  // tile, stages [k0, k1)
+};
+// Next segment of the descending walk from u down to u0 (false when done).
+__device__ __forceinline__ bool sk_next(uint32_t &u, uint32_t u0, uint32_t nk, SkSeg &sg) {
+  if (u <= u0) return false;
+  const uint32_t t = (u - 1) / nk, base = t * nk;
+  sg.t = t;
+  sg.k1 = u - base;
+  sg.k0 = u0 > base ? u0 - base : 0u;
+  u = base + sg.k0;
+  return true;
+}
+__device__ __forceinline__ uint32_t sk_u0(uint32_t p, uint32_t units, uint32_t pairs) {
+  return (uint32_t)(((uint64_t)p * units) / pairs);
+}
+// Bounded wait for a flag word to reach `epoch` (acquire: the partial it
+// guards is visible after it); false after the limit.
+__device__ __forceinline__ bool sk_wait_flag(const uint32_t *f, uint32_t epoch) {
+  for (uint32_t it = 0; it < kTcWaitLimit; ++it) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+    if (v == epoch) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(kPairThreads, 1)
+    gemm_tc_pair_streamk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                                SkArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  griddep_launch_dependents();
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t peer = cluster_rank() & 1u;  // clusters of 2: rank 0 leads
+  constexpr uint16_t kPairMask = 3;
+  constexpr uint32_t stage_bytes = 2 * kPairHalfBytes;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + a.stages * stage_bytes);
+  const uint32_t full = smem_u32(bars), empty = full + 8 * a.stages, acc_full = empty + 8 * a.stages;
+  const uint32_t acc_empty = acc_full + 16, mma_done = acc_empty + 16;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * a.stages + 5);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const uint32_t npairs = gridDim.x >> 1, pid = blockIdx.x >> 1, nk = a.nk;
+  const uint32_t u0 = sk_u0(pid, a.units, npairs), u1 = sk_u0(pid + 1, a.units, npairs);
+
+  if (tid == 0) {
+    for (int i = 0; i < a.stages; i++) {
+      mbar_init(full + 8 * i, 1);
+      mbar_init(empty + 8 * i, 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(acc_full + 8 * b, 1);
+      mbar_init(acc_empty + 8 * b, 8);  // 4 epilogue warps x 2 CTAs
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "n"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  griddep_wait();  // operands, result and workspace belong to the previous kernels until here
+
+  if (warp == 0) {
+    if (lane == 0 && peer == 0) {  // the leader's TMA: both CTAs' halves of every stage
+      uint32_t g = 0, u = u1;
+      bool stop = false;
+      SkSeg sg;
+      while (!stop && sk_next(u, u0, nk, sg)) {
+        const uint32_t m0 = (sg.t % a.mt) * 256u, n0 = (sg.t / a.mt) * 256u;
+        for (uint32_t k = sg.k0; k < sg.k1; k++, g++) {
+          const uint32_t s = g % a.stages, use = g / a.stages;
+          if (use > 0 && !mbar_wait(empty + 8 * s, (use - 1) & 1, abort_flag)) {
+            stop = true;
+            break;
+          }
+          const uint32_t fb = map_to_rank(full + 8 * s, 0);
+          mbar_expect_tx(full + 8 * s, 2 * stage_bytes);
+          const uint32_t dst = smem_u32(smem + s * stage_bytes), pdst = map_to_rank(dst, 1);
+          tma_load_digits_pair(dst, &tmA, (int)k, m0, fb);
+          tma_load_digits_pair(dst + kPairHalfBytes, &tmB, (int)k, n0, fb);
+          tma_load_digits_pair(pdst, &tmA, (int)k, m0 + 128, fb);
+          tma_load_digits_pair(pdst + kPairHalfBytes, &tmB, (int)k, n0 + 128, fb);
+        }
+      }
+      if (*abort_flag)  // wait (bounded) for the loads the barriers still expect
+        for (uint32_t q = (g > (uint32_t)a.stages ? g - a.stages : 0); q < g; q++)
+          mbar_drain(full + 8 * (q % a.stages), (q / a.stages) & 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && peer == 0) {  // the leader issues the pair's MMAs
+      bool ok = true;
+      uint32_t g = 0, j = 0, u = u1;
+      SkSeg sg;
+      while (ok && sk_next(u, u0, nk, sg)) {
+        const uint32_t b = j & 1u, dacc = tmem + b * 256u;
+        if (j >= 2 && !mbar_wait(acc_empty + 8 * b, ((j >> 1) - 1) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        for (uint32_t k = sg.k0; k < sg.k1; k++, g++) {
+          const uint32_t s = g % a.stages;
+          if (!mbar_wait(full + 8 * s, (g / a.stages) & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t base = smem_u32(smem + s * stage_bytes);
+#pragma unroll
+          for (int kk = 0; kk < 4; kk++)
+            mma_f8_pair(dacc, sw128_desc(base + kk * 32), sw128_desc(base + kPairHalfBytes + kk * 32), a.idesc,
+                        (k != sg.k0 || kk != 0) ? 1u : 0u);
+          mma_commit_pair(empty + 8 * s, kPairMask);
+        }
+        if (ok) mma_commit_pair(acc_full + 8 * b, kPairMask);
+        j++;
+      }
+      if (!ok) {  // issued MMAs finish before TMEM is freed
+        asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mma_done)
+                     : "memory");
+        mbar_drain(mma_done, 0);
+      }
+    }
+  } else {  // epilogue: this CTA's 128 rows of every segment
+    const int q = warp & 3;
+    const uint32_t row = 128u * peer + (uint32_t)(q * 32 + lane);  // row within the 256-row tile
+    uint32_t j = 0, u = u1;
+    SkSeg sg;
+    while (sk_next(u, u0, nk, sg)) {
+      const uint32_t b = j & 1u;
+      if (!__all_sync(0xffffffffu, mbar_wait(acc_full + 8 * b, (j >> 1) & 1, abort_flag))) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t taddr = tmem + b * 256u + ((uint32_t)(q * 32) << 16);
+      if (sg.k1 < nk) {
+        // a share of a tile a higher pair finishes: publish it as an fp32 partial
+        float *w = a.ws + (size_t)pid * 65536u + row;
+#pragma unroll 1
+        for (int col = 0; col < 256; col += 32) {
+          uint32_t v[32];
+          tmem_ld32(taddr + (uint32_t)col, v);
+          tmem_wait_ld(v);
+#pragma unroll
+          for (int i = 0; i < 32; i++) __stcg(w + (size_t)(col + i) * 256u, __uint_as_float(v[i]));
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) {
+          uint32_t *f = a.flags + pid * 8u + peer * 4u + (uint32_t)q;
+          asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(f), "r"(a.epoch) : "memory");
+        }
+      } else {
+        // this pair finishes the tile: add the partials of the lower pairs holding stages [0, k0)
+        const uint64_t gm = (uint64_t)(sg.t % a.mt) * 256u + row;
+        const uint64_t n0 = (uint64_t)(sg.t / a.mt) * 256u;
+        const uint32_t base = sg.t * nk;
+        uint32_t qlo = pid;  // contributors are pairs [qlo, pid)
+        bool ok = true;
+        for (uint32_t lo = sg.k0; lo > 0 && qlo > 0;) {
+          qlo--;
+          ok = ok && sk_wait_flag(a.flags + qlo * 8u + peer * 4u + (uint32_t)q, a.epoch);
+          const uint32_t uq = sk_u0(qlo, a.units, npairs);
+          lo = uq > base ? uq - base : 0u;
+        }
+        if (!__all_sync(0xffffffffu, ok)) {
+          if (lane == 0) atomicOr(&g_tc_error, 4u);
+          *abort_flag = 1;
+        }
+#pragma unroll 1
+        for (int col = 0; col < 256; col += 32) {
+          uint32_t v[32];
+          tmem_ld32(taddr + (uint32_t)col, v);
+          tmem_wait_ld(v);
+          float acc[32];
+#pragma unroll
+          for (int i = 0; i < 32; i++) acc[i] = __uint_as_float(v[i]);
+          for (uint32_t qq = qlo; qq < pid; qq++) {
+            const float *w = a.ws + (size_t)qq * 65536u + (size_t)col * 256u + row;
+#pragma unroll
+            for (int i = 0; i < 32; i++) acc[i] += __ldcg(w + (size_t)i * 256u);
+          }
+          int32_t o[32];
+#pragma unroll
+          for (int i = 0; i < 32; i++) o[i] = __float2int_rn(acc[i]);
+          store_result_cols<32>(a.C, a.M, a.N, gm, n0 + (uint64_t)col, o);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) {  // this warp is done with the buffer: tell the leader's MMA thread
+        if (peer == 0) {
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acc_empty + 8 * b) : "memory");
+        } else {
+          const uint32_t rb = map_to_rank(acc_empty + 8 * b, 0);
+          asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(rb) : "memory");
+        }
+      }
+      j++;
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -1127,7 +1429,20 @@ cudaError_t with_pair_kernel(int splits, int bn, F f) {
   return f(gemm_tc_pair_kernel<1, 256>);
 }
 
-void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1], int splits, int bn, size_t smem,
+// Programmatic stream serialization for a launch on `s`: on unless GBS_PDL=0,
+// the stream is the legacy default stream (which synchronises with others) or
+// the stream is being captured (graph launches keep plain edges).
+bool pdl_for(cudaStream_t s) {
+  if (!pdl_enabled() || s == nullptr) return false;
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return st == cudaStreamCaptureStatusNone;
+}
+
+void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[2], int splits, int bn, size_t smem,
                         cudaStream_t s) {
   with_pair_kernel(splits, bn, [&](auto kern) {
     return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1140,8 +1455,10 @@ void pair_launch_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute (&attr)[1],
   attr[0].val.clusterDim.x = 2 * splits;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl_for(s) ? 2 : 1;
 }
 
 // Clusters of 2 * splits CTAs that fit the GPU at once (they are placed within
@@ -1154,8 +1471,9 @@ int pair_max_clusters(int splits, int bn) {
   int v = slot.load(std::memory_order_relaxed);
   if (v == 0) {
     cudaLaunchConfig_t cfg;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     pair_launch_config(cfg, attr, splits, bn, pair_smem_bytes(bn), nullptr);
+    cfg.numAttrs = 1;
     cfg.gridDim = dim3(2 * splits, 1, 1);
     int n = 0;
     cudaError_t e = with_pair_kernel(splits, bn, [&](auto kern) { return cudaOccupancyMaxActiveClusters(&n, kern, &cfg); });
@@ -1177,7 +1495,128 @@ int pair_splits(uint64_t tiles, uint32_t nstages, int bn) {
   return 1;
 }
 
+// Shared memory of the persistent and stream-K pair kernels (256-column
+// tiles, two TMEM accumulators) and their ring depth.
+int pair_loop_stages() {
+  int stages = pair_stages(256);
+  while (stages > 2 && 1024 + (size_t)stages * 2 * kPairHalfBytes + 8 * (2 * stages + 5) + 16 > kPairSmemCap) stages--;
+  return stages;
+}
+size_t pair_loop_smem(int stages) { return 1024 + (size_t)stages * 2 * kPairHalfBytes + 8 * (2 * stages + 5) + 16; }
+
+// SM pairs the stream-K kernel can hold at once (its clusters of 2 are placed
+// within one GPC each), cached per device; every pair of a launch must be
+// resident together, since a tile's last pair waits for lower pairs' partials.
+int streamk_max_pairs() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
+    const size_t smem = pair_loop_smem(pair_loop_stages());
+    int n = 0;
+    if (cudaFuncSetAttribute(gemm_tc_pair_streamk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+        cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = 2;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(2);
+      cfg.blockDim = dim3(kPairThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      if (cudaOccupancyMaxActiveClusters(&n, gemm_tc_pair_streamk_kernel, &cfg) != cudaSuccess) n = 0;
+    }
+    cudaGetLastError();
+    v = n > 0 ? n : -1;
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v > 0 ? v : 0;
+}
+
+// Minimum K stages per pair for a stream-K launch: fewer pairs than the GPU
+// holds when the whole GEMM has too few units to give each pair this many.
+constexpr uint32_t kStreamKMinUnits = 8;
+
+// Launches the stream-K pair kernel over the context's digit matrices
+// (maps ready); allocates its workspace on first use.
+cudaError_t launch_pair_streamk(gbs_ctx *c, cudaStream_t s, const TmaArgs &ta) {
+  const uint64_t mt = (ta.M + 255) / 256, nt = (ta.N + 255) / 256;
+  const uint64_t units = mt * nt * ta.nstages;
+  const int maxp = streamk_max_pairs();
+  if (maxp <= 0 || units == 0 || units > 0xFFFFFFFFull) return cudaErrorInvalidConfiguration;
+  const uint32_t pairs =
+      (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)maxp, units / kStreamKMinUnits));
+  if (c->sk_pairs < pairs) {
+    if (c->sk_ws) cudaFree(c->sk_ws);
+    if (c->sk_flags) cudaFree(c->sk_flags);
+    c->sk_ws = nullptr;
+    c->sk_flags = nullptr;
+    c->sk_pairs = 0;
+    cudaError_t e = dev_alloc((void **)&c->sk_ws, (size_t)pairs * 65536 * sizeof(float));
+    if (e == cudaSuccess) e = dev_alloc((void **)&c->sk_flags, (size_t)pairs * 8 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->sk_flags, 0, (size_t)pairs * 8 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    c->sk_pairs = pairs;
+    c->sk_epoch = 0;
+  }
+  if (++c->sk_epoch == 0) c->sk_epoch = 1;  // flags start at 0: epoch 0 is never a live launch
+  SkArgs a;
+  memset(&a, 0, sizeof(a));
+  a.C = ta.C;
+  a.ws = c->sk_ws;
+  a.flags = c->sk_flags;
+  a.M = ta.M;
+  a.N = ta.N;
+  a.nk = ta.nstages;
+  a.mt = (uint32_t)mt;
+  a.units = (uint32_t)units;
+  a.epoch = c->sk_epoch;
+  a.idesc = (1u << 4) | ((uint32_t)(256 >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
+  a.stages = pair_loop_stages();
+  const size_t smem = pair_loop_smem(a.stages);
+  cudaError_t e =
+      cudaFuncSetAttribute(gemm_tc_pair_streamk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = dim3(2 * pairs);
+  cfg.blockDim = dim3(kPairThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_for(s) ? 2 : 1;
+  const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
+  const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_db);
+  e = cudaLaunchKernelEx(&cfg, gemm_tc_pair_streamk_kernel, ma, mb, a);
+  count_launch();
+  c->last_pair_bn = 256;
+  c->last_pair_splits = 1;
+  c->last_pair_persistent = false;
+  c->last_pair_streamk = (int)pairs;
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
+
 }  // namespace
+
+// GBS_PDL=0 in the environment launches the tensor-core kernels without
+// programmatic stream serialization (read once per process).
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *v = getenv("GBS_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
 
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   for (int side = 0; side < 2; side++)
@@ -1210,7 +1649,9 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     if (!err) return cudaErrorInvalidSymbol;
     return tcg_gemm(*c->plan1, err, s, c->out);
   }
-  if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req == kPairVariantPersistent || bn_req < 0) {
+  if (bn_req == kPairVariantStreamK) return launch_pair_streamk(c, s, a);
+  if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req == kPairVariantPersistent || bn_req < 0 ||
+      pair_split_variant(bn_req)) {
     // 256 x BN tiles on SM pairs
     // Tile width and K split.  A split sums partials over distributed shared
     // memory, which costs more the more chunks there are: candidates in order
@@ -1221,6 +1662,13 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     const uint64_t mt = (a.M + 255) / 256;
     int bn = bn_req == kPairVariant128 ? 128 : 256;
     int splits = pair_splits(mt * ((a.N + bn - 1) / bn), a.nstages, bn);
+    if (pair_split_variant(bn_req)) {  // tile width and K split both forced (a tuner candidate)
+      bn = bn_req / 10;
+      splits = bn_req % 10;
+      const uint64_t tiles = mt * ((a.N + bn - 1) / bn);
+      if (splits > 1 && (a.nstages < (uint32_t)splits || tiles > (uint64_t)pair_max_clusters(splits, bn)))
+        splits = 1;  // every K chunk needs a stage, and all clusters of the grid must fit at once
+    }
     if (bn_req < 0) {
       const uint64_t pairs = (uint64_t)sm_count_cached() / 2;
       static const int cand[6][2] = {{256, 1}, {256, 2}, {128, 1}, {128, 2}, {256, 4}, {128, 4}};
@@ -1268,17 +1716,19 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
       if (e != cudaSuccess) return e;
       cudaLaunchConfig_t cfg;
       cfg = cudaLaunchConfig_t{};
-      cudaLaunchAttribute attr[1];
+      cudaLaunchAttribute attr[2];
       attr[0].id = cudaLaunchAttributeClusterDimension;
       attr[0].val.clusterDim.x = 2;
       attr[0].val.clusterDim.y = 1;
       attr[0].val.clusterDim.z = 1;
+      attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[1].val.programmaticStreamSerializationAllowed = 1;
       cfg.gridDim = dim3((unsigned)(2 * npairs));
       cfg.blockDim = dim3(kPairThreads);
       cfg.dynamicSmemBytes = smem;
       cfg.stream = s;
       cfg.attrs = attr;
-      cfg.numAttrs = 1;
+      cfg.numAttrs = pdl_for(s) ? 2 : 1;
       if (!c->digit_maps_ready) return cudaErrorInvalidValue;
       const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
       const CUtensorMap &mb = *reinterpret_cast<const CUtensorMap *>(c->tc_map_db);
@@ -1287,12 +1737,13 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
       c->last_pair_bn = 256;
       c->last_pair_splits = 1;
       c->last_pair_persistent = true;
+      c->last_pair_streamk = 0;
       return e != cudaSuccess ? e : cudaGetLastError();
     }
     a.stages = pair_stages(bn);
     const size_t smem = pair_smem_bytes(bn);
     cudaLaunchConfig_t cfg;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     pair_launch_config(cfg, attr, a.splits, bn, smem, s);
     cfg.gridDim = dim3((unsigned)(2 * a.splits * mt), (unsigned)((a.N + bn - 1) / bn));
     const CUtensorMap &ma = *reinterpret_cast<const CUtensorMap *>(c->tc_map_da);
@@ -1302,6 +1753,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
     c->last_pair_bn = bn;
     c->last_pair_splits = a.splits;
     c->last_pair_persistent = false;
+    c->last_pair_streamk = 0;
     return e != cudaSuccess ? e : cudaGetLastError();
   }
   const int bn = (bn_req == 128 || bn_req == 256) ? bn_req : (a.N > 128 ? 256 : 128);

@@ -183,6 +183,11 @@ struct gbs_ctx {
   bool digit_map_b64_ready = false;
   int last_pair_bn = 0, last_pair_splits = 0;  // configuration of the last SM-pair launch (test hook)
   bool last_pair_persistent = false;
+  int last_pair_streamk = 0;  // SM pairs of the last stream-K launch, 0 if the last pair launch was another kernel
+  // stream-K pair kernel: fp32 partial-tile slots and flags, one per SM pair, and the launch epoch
+  float *sk_ws = nullptr;
+  uint32_t *sk_flags = nullptr;
+  uint32_t sk_pairs = 0, sk_epoch = 0;
   // one-problem plan of the persistent tensor-core kernel (shapes with a side under 256 rows)
   gbs::TcgPlan *plan1 = nullptr;
   bool plan1_ready = false;
@@ -241,6 +246,12 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn);
 constexpr int kPairVariant = 512;     // tensor-core variant: 256 x 256 tiles on SM pairs (tcgen05 cta_group::2)
 constexpr int kPairVariant128 = 513;  // the same with 256 x 128 tiles
 constexpr int kPairVariantPersistent = 514;  // persistent SM pairs looping over 256 x 256 tiles
+constexpr int kPairVariantStreamK = 515;     // stream-K SM pairs: (tile, K stage) units split evenly over the pairs
+// SM-pair tiles with width and K split both given: 10 * width + split, width 128 or 256, split 1, 2 or 4
+inline bool pair_split_variant(int v) {
+  return (v == 1281 || v == 1282 || v == 1284 || v == 2561 || v == 2562 || v == 2564);
+}
+bool pdl_enabled();                          // programmatic dependent launch of the tensor-core kernels (GBS_PDL)
 uint32_t tc_error_word();
 int tc_peaks(double *f8, double *bf16);
 

@@ -51,6 +51,17 @@ __device__ __forceinline__ void mbar_drain_err(uint32_t bar, uint32_t parity, ui
   atomicOr(err, 2u);
 }
 
+// Programmatic dependent launch.  A kernel launched with the
+// programmatic-stream-serialization attribute may start while the kernel
+// before it in the stream is still running: it sets up (barriers, TMEM) and
+// then calls griddep_wait(), which returns once the previous grids have
+// completed and their memory is visible; nothing before it may read or write
+// global memory.  griddep_launch_dependents() lets the next such kernel in
+// the stream be scheduled as soon as every CTA of this one has issued it (its
+// CTAs then take SMs as ours leave and wait likewise).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(

@@ -288,7 +288,7 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
   struct Cand {
     int pipe, variant;
   };
-  Cand cands[16];
+  Cand cands[24];
   int nc = 0;
   for (int v = -1; v <= 2; v++) cands[nc++] = Cand{GBS_PIPE_POPC, v};  // -1: built-in tile rule
   cands[nc++] = Cand{GBS_PIPE_BMMA, -1};
@@ -296,9 +296,10 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
     cands[nc++] = Cand{GBS_PIPE_TC, -1};  // built-in rule: SM pairs, or the persistent kernel for a side < 256
     cands[nc++] = Cand{GBS_PIPE_TC, 128};
     cands[nc++] = Cand{GBS_PIPE_TC, 256};
-    cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant};
-    cands[nc++] = Cand{GBS_PIPE_TC, kPairVariant128};
     cands[nc++] = Cand{GBS_PIPE_TC, kPairVariantPersistent};
+    cands[nc++] = Cand{GBS_PIPE_TC, kPairVariantStreamK};
+    // SM-pair tiles: width 256 / 128 x K split 1, 2, 4
+    for (int v : {2561, 2562, 2564, 1281, 1282, 1284}) cands[nc++] = Cand{GBS_PIPE_TC, v};
   }
   if (tc_exact(c, GBS_PIPE_TC_SMEM)) {
     cands[nc++] = Cand{GBS_PIPE_TC_SMEM, 256};
@@ -337,6 +338,18 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
     g_store[key_of(c)] = best;
   }
   if (best_pipe) *best_pipe = best.pipe;
+  return GBS_OK;
+}
+
+extern "C" int gbs_tuner_lookup(const gbs_ctx *c, int *pipe, int *variant, double *us) {
+  if (!c || !pipe || !variant || !us) return fail(GBS_EINVAL, "gbs_tuner_lookup: NULL argument");
+  std::lock_guard<std::mutex> lock(g_store_mu);
+  load_env_store();
+  auto it = g_store.find(key_of(c));
+  if (it == g_store.end()) return fail(GBS_ESTATE, "gbs_tuner_lookup: no entry for this shape class");
+  *pipe = it->second.pipe;
+  *variant = it->second.variant;
+  *us = it->second.us;
   return GBS_OK;
 }
 

@@ -193,8 +193,13 @@ GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);
  * cta_group::2), K split over up to 4 pairs of one cluster when the tiles are
  * too few to fill the GPU, or 514: persistent SM pairs looping over
  * 256 x 256 tiles (about three per pair when forced; the built-in rule takes
- * them for grids of more tiles than one wave holds); -1 restores the
- * built-in rule.  No reference counterpart. */
+ * them for grids of more tiles than one wave holds), or 515: stream-K SM
+ * pairs, the (256 x 256 tile, K stage) units split evenly over every pair the
+ * GPU holds at once, split tiles summed through a per-context workspace, or
+ * 10 * width + split (1281, 1282, 1284, 2561, 2562, 2564): SM-pair tiles of
+ * that width with K split over that many pairs of a cluster (a split that
+ * cannot run -- fewer K stages than chunks, too many clusters -- runs as 1);
+ * -1 restores the built-in rule.  No reference counterpart. */
 GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
 
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
@@ -321,6 +326,9 @@ GBS_API int gbs_tuner_save(const char *path);
 GBS_API int gbs_tuner_load(const char *path, int replace);
 GBS_API int gbs_tuner_entries(void);
 GBS_API int gbs_tuner_clear(void);
+/* The store's entry for ctx's shape class: its pipe, variant and the time
+ * gbs_tune measured (us); GBS_ESTATE when the store has none. */
+GBS_API int gbs_tuner_lookup(const gbs_ctx *ctx, int *pipe, int *variant, double *us);
 
 /* Message describing the last failure on the calling thread ("" if none). */
 GBS_API const char *gbs_last_error(void);
@@ -343,8 +351,10 @@ GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 /* Number of kernel launches the library has issued since load (all entry points). */
 GBS_API uint64_t gbs_debug_launch_count(void);
 
-/* Tile width (256 or 128), K split (1, 2 or 4) and whether the persistent
- * kernel ran (1) for the last SM-pair launch of ctx; all 0 if none was. */
+/* Tile width (256 or 128), K split (1, 2 or 4; for the stream-K kernel the
+ * number of SM pairs it ran on) and which SM-pair kernel ran for the last
+ * SM-pair launch of ctx: 0 one tile per pair, 1 the persistent kernel, 2 the
+ * stream-K kernel; all 0 if none was. */
 GBS_API int gbs_debug_last_pair(const gbs_ctx *ctx, int *bn, int *splits, int *persistent);
 
 #ifdef __cplusplus

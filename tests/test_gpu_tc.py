@@ -289,3 +289,82 @@ def test_pair_auto_goes_persistent_past_one_wave():
         assert last_pair(ctx, True) == (256, 1, 1)
     finally:
         deallocGEMMContext(ctx)
+
+
+# stream-K shapes: tiles split over 2, 3 and 5 pairs, and an uneven split over every pair the GPU holds
+STREAMK_CASES = [(300, 2000, 600), (700, 3000, 900), (257, 5000, 513), (1024, 8192, 1024)]
+
+
+@pytest.mark.parametrize("shape", STREAMK_CASES, ids=[f"{m}x{k}x{n}" for (m, k, n) in STREAMK_CASES])
+def test_pair_streamk(shape):
+    """Stream-K SM pairs (variant 515): (tile, K stage) units split evenly over the pairs, split tiles
+    finished by the pair holding their last stage from the lower pairs' fp32 partials; a second
+    launch over the same context (the next epoch of the partials' flags) gives the same bits."""
+    M, K, N = shape
+    rng = np.random.default_rng(M + 7 * K + 11 * N)
+    for (wa, ea, wb, eb) in [(3, "u", 2, "s"), (1, "b", 1, "b"), (4, "s", 1, "u")]:
+        A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+        B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+        sa, sb = ea != "u", eb != "u"
+        ctx = allocGEMMContext(M, K, N, wa, wb, sa, sb)
+        try:
+            _capi.check(_capi.load().gbs_set_variant(ctx._h, 515))
+            ctx.set_pipe(_capi.GBS_PIPE_TC)
+            ctx.lhs.importRegular(A)
+            ctx.rhs.importRegular(B)
+            gemmBitSerial(ctx)
+            got = ctx.res.reshape(N, M).copy()
+            bn, pairs, kind = last_pair(ctx, True)
+            assert (bn, kind) == (256, 2) and pairs >= 1
+            gemmBitSerial(ctx)
+            assert np.array_equal(ctx.res.reshape(N, M), got)
+        finally:
+            deallocGEMMContext(ctx)
+        assert np.array_equal(got, O.oracle_gemm(A, B, wa, wb, sa, sb, threads=8)), (shape, wa, ea, wb, eb)
+    assert _capi.load().gbs_debug_tc_error() == 0
+
+
+@pytest.mark.parametrize("name", ["gemm_2048x4096x2048_u3s2", "gemm_256x9216x4096_bpbp", "gemm_256x9216x4096_bps4",
+                                  "gemm_4096x2048x2048_u2bp"])
+def test_pair_streamk_full_size(name):
+    """The full-size workloads on the stream-K kernel: the reference's result bits."""
+    M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+    ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+    try:
+        _capi.check(_capi.load().gbs_set_variant(ctx._h, 515))
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        for _ in range(2):
+            gemmBitSerial(ctx)
+            assert sha(ctx.res.reshape(N, M)) == CFG[name]["sha256"]
+        bn, pairs, kind = last_pair(ctx, True)
+        assert (bn, kind) == (256, 2) and pairs >= 1
+    finally:
+        deallocGEMMContext(ctx)
+    assert _capi.load().gbs_debug_tc_error() == 0
+
+
+# explicit tile width x K split variants (a split that cannot run falls back to 1)
+SPLIT_VARIANTS = [(2561, 256, 1), (2562, 256, 2), (2564, 256, 4), (1281, 128, 1), (1282, 128, 2), (1284, 128, 4)]
+
+
+@pytest.mark.parametrize("case", SPLIT_VARIANTS, ids=[str(c[0]) for c in SPLIT_VARIANTS])
+def test_pair_explicit_split_variants(case):
+    variant, bn_want, split_want = case
+    M, K, N = 512, 4096, 512
+    rng = np.random.default_rng(variant)
+    A = datagen.operand(int(rng.integers(1 << 30)), M, K, 3, "u")
+    B = datagen.operand(int(rng.integers(1 << 30)), N, K, 2, "s")
+    ctx = allocGEMMContext(M, K, N, 3, 2, False, True)
+    try:
+        _capi.check(_capi.load().gbs_set_variant(ctx._h, variant))
+        ctx.set_pipe(_capi.GBS_PIPE_TC)
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        gemmBitSerial(ctx)
+        got = ctx.res.reshape(N, M).copy()
+        assert last_pair(ctx, True) == (bn_want, split_want, 0)
+    finally:
+        deallocGEMMContext(ctx)
+    assert np.array_equal(got, O.oracle_gemm(A, B, 3, 2, False, True))

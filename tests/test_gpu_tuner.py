@@ -46,7 +46,8 @@ def test_tune_records_winner_and_stays_exact(gbs_lib, tmp_path):
 
 CANDIDATES = [(_capi.GBS_PIPE_POPC, v) for v in (-1, 0, 1, 2)] + [(_capi.GBS_PIPE_BMMA, -1)] + \
     [(_capi.GBS_PIPE_TC, 128), (_capi.GBS_PIPE_TC, 256), (_capi.GBS_PIPE_TC_SMEM, 128), (_capi.GBS_PIPE_TC_SMEM, 256),
-     (_capi.GBS_PIPE_TC_PAIRS, 128), (_capi.GBS_PIPE_TC_PAIRS, 256)]
+     (_capi.GBS_PIPE_TC_PAIRS, 128), (_capi.GBS_PIPE_TC_PAIRS, 256)] + \
+    [(_capi.GBS_PIPE_TC, v) for v in (-1, 512, 513, 514, 515, 2561, 2562, 2564, 1281, 1282, 1284)]
 
 
 def test_every_candidate_is_exact(gbs_lib):
@@ -86,3 +87,30 @@ def test_tuned_variants_are_exact(gbs_lib):
         assert np.array_equal(ctx.res.reshape(N, M), want), (M, K, N, best.value)
         deallocGEMMContext(ctx)
     lib.gbs_tuner_clear()
+
+
+def test_committed_store_covers_the_workloads_and_stays_exact(gbs_lib):
+    """The GB300 tuner store committed with the library (gemmbitserial_gb300/tuned, written by
+    gemmbitserial_gb300.tune_workloads) has an entry for every named workload, and the kernels it
+    picks give the reference's result bits."""
+    lib = gbs_lib
+    store = os.path.join(os.path.dirname(GOLD), "..", "gemmbitserial_gb300", "tuned", "gb300_sm103a.txt")
+    _capi.check(lib.gbs_tuner_load(os.path.abspath(store).encode(), 1))
+    cfg = json.load(open(os.path.join(GOLD, "ref_configs.json")))
+    try:
+        for name in datagen.WORKLOADS:
+            M, K, N, wA, sA, wB, sB, A, B = datagen.workload(name)
+            ctx = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+            try:
+                pipe, var, us = C.c_int(), C.c_int(), C.c_double()
+                _capi.check(lib.gbs_tuner_lookup(ctx._h, C.byref(pipe), C.byref(var), C.byref(us)))
+                assert ctx.pipe == pipe.value and us.value > 0, name
+                ctx.lhs.importRegular(A)
+                ctx.rhs.importRegular(B)
+                gemmBitSerial(ctx)
+                got = ctx.res.reshape(N, M)
+                assert hashlib.sha256(np.ascontiguousarray(got).tobytes()).hexdigest() == cfg[name]["sha256"], name
+            finally:
+                deallocGEMMContext(ctx)
+    finally:
+        lib.gbs_tuner_clear()
