@@ -25,3 +25,18 @@ def test_store_roundtrip_and_version_check(gbs_lib, tmp_path):
     assert lib.gbs_tuner_entries() == 2
     assert lib.gbs_tuner_load(str(tmp_path / "missing.txt").encode(), 0) == _capi.GBS_EINVAL
     assert lib.gbs_tuner_clear() == _capi.GBS_OK and lib.gbs_tuner_entries() == 0
+
+
+def test_committed_gb300_store_parses():
+    """The committed store is in the current format: a version line, then entries of 7 key integers,
+    a pipe, a variant and a time, one for every named workload's shape class."""
+    import os
+
+    from gemmbitserial_gb300 import datagen
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lines = open(os.path.join(root, "gemmbitserial_gb300", "tuned", "gb300_sm103a.txt")).read().splitlines()
+    assert lines[0] == "gbs-tuner v1 sm_103a"
+    entries = [l.split() for l in lines[1:] if l.strip()]
+    assert len(entries) == len(datagen.WORKLOADS)  # the named workloads have distinct shape classes
+    for e in entries:
+        assert len(e) == 10 and 1 <= int(e[7]) <= 5 and float(e[9]) > 0
