@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbs_debug_fail_alloc_after": (None, [i32]),
     "gbs_debug_launch_count": (u64, []),
     "gbs_debug_last_pair": (i32, [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "gbs_debug_tc_timeout": (i32, [vp, C.c_uint32, vp]),
     "gbs_debug_tc_error": (C.c_uint32, []),
 }
 

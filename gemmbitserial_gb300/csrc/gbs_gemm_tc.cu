@@ -74,6 +74,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
   return mbar_wait_err(bar, parity, abort_flag, &g_tc_error);
 }
 __device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) { mbar_drain_err(bar, parity, &g_tc_error); }
+// mbar_wait with a given number of rounds (the test hook's short limit)
+__device__ __forceinline__ bool mbar_wait_rounds(uint32_t bar, uint32_t parity, volatile int *abort_flag,
+                                                 uint32_t rounds) {
+  for (uint32_t it = 0; it < rounds; ++it) {
+    if (mbar_try(bar, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  atomicOr(&g_tc_error, 1u);
+  return false;
+}
 
 // One tile row of one stage: CNT planes (16 bytes each, `pstride` apart) ->
 // 128 e4m3 bytes written as 8 swizzled 16-byte chunks.  Columns at or past
@@ -294,6 +305,10 @@ struct TmaArgs {
   uint32_t idesc;
   int stages;
   int splits;  // SM-pair kernel: K chunks per output tile, one SM pair each (1, 2 or 4)
+  // SM-pair kernel, test hook: 0 normally; otherwise nothing is loaded or
+  // multiplied and the waits give up after this many rounds, so the kernel
+  // takes its abort path (error bit, drains, TMEM freed) and returns
+  uint32_t wait_limit;
 };
 
 template <int BN>
@@ -538,11 +553,11 @@ __global__ void __launch_bounds__(kPairThreads, 1)
   const uint32_t nk = k_hi - k_lo;
   bool tile_done = false;  // epilogue warps: the accumulator is complete
   griddep_launch_dependents();
-  if (tid == 0) {  // descriptors towards the TMA unit before the first load needs them
+  if (tid == 0 && a.wait_limit == 0) {  // descriptors towards the TMA unit before the first load needs them
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
   }
-  if (tid == 64 && peer == 0) {
+  if (tid == 64 && peer == 0 && a.wait_limit == 0) {
     // an epilogue thread (idle until the accumulator is done) sends the first
     // three stages towards L2 while setup runs and the previous kernel
     // finishes: about 50 ns per hint, within the setup's own time (issued
@@ -585,8 +600,8 @@ __global__ void __launch_bounds__(kPairThreads, 1)
     // peer's into the peer's shared memory, all completing on the leader's
     // full barrier.  Each CTA loading its own halves onto that barrier puts a
     // cross-SM completion on every stage's critical path, which measured about
-    // twice as slow per stage as the one-issuer ring.
-    if (lane == 0 && peer == 0) {
+    // twice as slow per stage as the one-issuer ring.  (The test hook loads nothing.)
+    if (lane == 0 && peer == 0 && a.wait_limit == 0) {
       uint32_t issued = 0;
       for (uint32_t k = 0; k < nk; k++) {
         const uint32_t s = k % a.stages, use = k / a.stages;
@@ -611,7 +626,8 @@ __global__ void __launch_bounds__(kPairThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0 && peer == 0) {
-      bool ok = true;
+      // test hook: nothing was loaded, so this wait runs out (no copy or MMA in flight)
+      bool ok = a.wait_limit == 0 || mbar_wait_rounds(full, 0, abort_flag, a.wait_limit);
       for (uint32_t k = 0; k < nk && ok; k++) {
         const uint32_t s = k % a.stages;
         if (!mbar_wait(full + 8 * s, (k / a.stages) & 1, abort_flag)) {
@@ -635,7 +651,8 @@ __global__ void __launch_bounds__(kPairThreads, 1)
       }
     }
   } else {
-    tile_done = __all_sync(0xffffffffu, mbar_wait(acc_full, 0, abort_flag));
+    tile_done = __all_sync(0xffffffffu, a.wait_limit ? mbar_wait_rounds(acc_full, 0, abort_flag, a.wait_limit)
+                                                     : mbar_wait(acc_full, 0, abort_flag));
     if (tile_done) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int q = warp & 3;
@@ -1741,6 +1758,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
       return e != cudaSuccess ? e : cudaGetLastError();
     }
     a.stages = pair_stages(bn);
+    a.wait_limit = c->debug_wait_limit;
     const size_t smem = pair_smem_bytes(bn);
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[2];
@@ -1861,3 +1879,45 @@ uint32_t tc_error_word() {
 }
 
 }  // namespace gbs
+
+using namespace gbs;
+
+// Test hook of the tensor-core kernels' bounded waits: one launch of the
+// SM-pair kernel that loads and multiplies nothing, so its first wait gives up
+// after `rounds` try_wait rounds; the kernel then takes its abort path (error
+// bit, bounded drains, TMEM freed, clean exit) and the host reads the error.
+extern "C" int gbs_debug_tc_timeout(gbs_ctx *c, uint32_t rounds, void *stream) {
+  if (!c || rounds == 0) return fail(GBS_EINVAL, "gbs_debug_tc_timeout: NULL context or zero rounds");
+  if (!c->lhs.imported || !c->rhs.imported) return fail(GBS_ESTATE, "gbs_debug_tc_timeout: import both operands first");
+  if (!tc_exact(c, GBS_PIPE_TC) || c->lhs.nrows < 256 || c->rhs.nrows < 256)
+    return fail(GBS_EUNSUPPORTED, "gbs_debug_tc_timeout: needs a context the SM-pair kernel runs (M, N >= 256)");
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(c->device) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "gbs_debug_tc_timeout: cudaSetDevice");
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t zero = 0;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(zero));
+  const int saved_pipe = c->pipe, saved_variant = c->variant;
+  int rc = GBS_OK;
+  if (e == cudaSuccess) {
+    c->pipe = GBS_PIPE_TC;
+    c->variant = 2561;  // one 256 x 256 tile per SM pair, no K split
+    c->debug_wait_limit = rounds;
+    rc = gbs_gemm(c, stream);
+    c->debug_wait_limit = 0;
+    c->pipe = saved_pipe;
+    c->variant = saved_variant;
+    e = cudaStreamSynchronize(s);
+  }
+  uint32_t err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&err, g_tc_error, sizeof(err));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(zero));
+  if (prev >= 0) cudaSetDevice(prev);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_debug_tc_timeout");
+  if (rc != GBS_OK) return rc;
+  if (err) return fail(GBS_ETIMEOUT, "gbs_debug_tc_timeout: the kernel's bounded wait gave up (error bits " +
+                                         std::to_string(err) + "); it drained, freed TMEM and returned");
+  return fail(GBS_EINVAL, "gbs_debug_tc_timeout: the wait did not run out");
+}
+

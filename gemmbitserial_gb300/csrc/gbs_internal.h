@@ -183,7 +183,8 @@ struct gbs_ctx {
   bool digit_map_b64_ready = false;
   int last_pair_bn = 0, last_pair_splits = 0;  // configuration of the last SM-pair launch (test hook)
   bool last_pair_persistent = false;
-  int last_pair_streamk = 0;  // SM pairs of the last stream-K launch, 0 if the last pair launch was another kernel
+  int last_pair_streamk = 0;
+  uint32_t debug_wait_limit = 0;  // test hook of gbs_debug_tc_timeout (0: normal launches)  // SM pairs of the last stream-K launch, 0 if the last pair launch was another kernel
   // stream-K pair kernel: fp32 partial-tile slots and flags, one per SM pair, and the launch epoch
   float *sk_ws = nullptr;
   uint32_t *sk_flags = nullptr;

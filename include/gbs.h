@@ -348,6 +348,16 @@ GBS_API uint32_t gbs_debug_tc_error(void);
  * exercise the grouped kernel's descriptor validation (host-side injection). */
 GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 
+/* Exercises the tensor-core kernels' bounded waits without a GPU fault: one
+ * launch of the SM-pair kernel over ctx (an imported context of M, N >= 256
+ * whose widths the tensor cores cover) that loads and multiplies nothing, so
+ * its first mbarrier wait gives up after `rounds` try_wait rounds.  The kernel
+ * then takes the abort path every such wait has -- error bit, bounded drains,
+ * TMEM freed, return -- and this call returns GBS_ETIMEOUT once the stream is
+ * idle, with the error word cleared again and the context usable.  The
+ * result buffer is not written.  No reference counterpart. */
+GBS_API int gbs_debug_tc_timeout(gbs_ctx *ctx, uint32_t rounds, void *stream);
+
 /* Number of kernel launches the library has issued since load (all entry points). */
 GBS_API uint64_t gbs_debug_launch_count(void);
 
