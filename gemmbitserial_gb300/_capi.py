@@ -32,6 +32,8 @@ class CtxInfo(C.Structure):
 SIGNATURES = {
     "gbs_ctx_alloc": (i32, [u64, u64, u64, u64, u64, i32, i32, C.POINTER(vp)]),
     "gbs_ctx_allocate": (i32, [u64, u64, u64, u64, u64, i32, i32, C.POINTER(vp)]),
+    "gbs_ctx_dims": (i32, [u64, u64, u64, C.POINTER(u64)]),
+    "gbs_matrix_alloc": (i32, [u64, u64, u64, i32, u64, u64, C.POINTER(vp)]),
     "gbs_ctx_free": (i32, [vp]),
     "gbs_ctx_get_info": (i32, [vp, C.POINTER(CtxInfo)]),
     "gbs_import": (i32, [vp, i32, vp, i32, i32, vp]),

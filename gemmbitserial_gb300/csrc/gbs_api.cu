@@ -7,6 +7,7 @@
 // (prepareAccumulators_generic, :39-76; usingBinary weights, :179-192;
 // bipolar correction, :255-259), result read-back and deallocation.
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -132,6 +133,69 @@ void free_ctx_buffers(gbs_ctx *c) {
   if (c->digits[1]) cudaFree(c->digits[1]);
 }
 
+// The reference's padding of a context's bit planes, restated:
+// allocGEMMContext_generic (arch-generic.hpp:78-100) picks the register
+// blocking (2 x 1 x 2 words, or 1 x 4 x 1 for matrix-vector contexts, whose
+// depth aligns to 256 bits) and a 32 KiB cache budget; allocGEMMContext_base
+// (gemmbitserial.hpp:415-452) turns them into cache blocks with
+// computeBlockSize (:343-360, the positive root of a quadratic in single
+// precision, as the reference computes it) and finetuneBlockSize (:364-377),
+// and BitSerialMatrix::alloc (:24-35) pads rows to the block and columns to
+// 64 bits times the depth blocking.  Empty sides (M or N = 0, where the
+// reference divides by zero) pad to nothing.
+struct Geometry {
+  uint64_t lhs_rows = 0, rhs_rows = 0, cols = 0, lhs_block = 0, rhs_block = 0;
+};
+
+void block_size(float lm, float rm, float cache_bits, float dbits, uint64_t &lb, uint64_t &rb) {
+  const float qa = (float)sizeof(int32_t) * lm * rm, qb = dbits * (lm + rm), qc = -cache_bits;
+  const float disc = sqrtf(qb * qb - 4.0f * qa * qc);
+  const int64_t x0 = (int64_t)floorf((-qb + disc) / (2.0f * qa)), x1 = (int64_t)floorf((-qb - disc) / (2.0f * qa));
+  const int64_t x = x0 > x1 ? x0 : x1;
+  if (x > 0) {
+    lb = (uint64_t)(lm * (float)x);
+    rb = (uint64_t)(rm * (float)x);
+  } else {
+    lb = (uint64_t)lm;
+    rb = (uint64_t)rm;
+  }
+}
+
+uint64_t finetune_block(uint64_t rows, uint64_t bs_max, uint64_t div) {
+  uint64_t best = bs_max, waste = round_up(rows, bs_max) - rows;
+  for (uint64_t cand = bs_max; cand > div; cand -= div) {
+    if (cand % div) continue;
+    const uint64_t wst = round_up(rows, cand) - rows;
+    if (wst < waste) {
+      best = cand;
+      waste = wst;
+    }
+  }
+  return best;
+}
+
+Geometry reference_geometry(uint64_t M, uint64_t K, uint64_t N) {
+  const uint64_t rl = N == 1 ? 1 : 2, rd = N == 1 ? 4 : 1, rr = N == 1 ? 1 : 2;
+  const float cache_bits = 32.0f * 1024.0f * 8.0f;
+  Geometry g;
+  const uint64_t kal = round_up(K, rd * 64);
+  block_size((float)rl, (float)rr, cache_bits, (float)kal, g.lhs_block, g.rhs_block);
+  if (g.lhs_block > M || g.rhs_block > N) {
+    g.lhs_block = round_up(M, rl);
+    g.rhs_block = round_up(N, rr);
+  } else {
+    if ((double)(round_up(M, g.lhs_block) - M) > 0.1 * (double)M) g.lhs_block = finetune_block(M, g.lhs_block, rl);
+    if ((double)(round_up(N, g.rhs_block) - N) > 0.1 * (double)N) g.rhs_block = finetune_block(N, g.rhs_block, rr);
+  }
+  g.lhs_rows = round_up(M, g.lhs_block);
+  g.rhs_rows = round_up(N, g.rhs_block);
+  g.cols = round_up(K, rd * 64);
+  return g;
+}
+
+int alloc_context(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB, const Geometry &geo,
+                  gbs_ctx **out, const char *who);
+
 // Epilogue and operand order for one context (see gbs_internal.h: Epilogue).
 }  // namespace
 
@@ -200,32 +264,71 @@ int gbs_debug_last_pair(const gbs_ctx *c, int *bn, int *splits, int *persistent)
 
 int gbs_tc_peaks(double *f8_flops, double *bf16_flops) { return tc_peaks(f8_flops, bf16_flops); }
 
+int gbs_ctx_dims(uint64_t M, uint64_t K, uint64_t N, uint64_t *dims) {
+  if (!dims) return fail(GBS_EINVAL, "gbs_ctx_dims: dims is NULL");
+  const Geometry g = reference_geometry(M, K, N);
+  dims[0] = g.lhs_rows;
+  dims[1] = g.rhs_rows;
+  dims[2] = g.cols;
+  dims[3] = g.cols;
+  dims[4] = g.lhs_block;
+  dims[5] = g.rhs_block;
+  return GBS_OK;
+}
+
 int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB,
                   gbs_ctx **out) {
-  if (!out) return fail(GBS_EINVAL, "gbs_ctx_alloc: out is NULL");
+  return alloc_context(M, K, N, wA, wB, sA, sB, reference_geometry(M, K, N), out, "gbs_ctx_alloc");
+}
+
+int gbs_matrix_alloc(uint64_t nbits, uint64_t nrows, uint64_t ncols, int issigned, uint64_t rowalign,
+                     uint64_t colalign, gbs_ctx **out) {
+  if (rowalign < 1 || colalign < 64 || colalign % 64)
+    return fail(GBS_EINVAL, "gbs_matrix_alloc: rowalign must be >= 1 and colalign a positive multiple of 64");
+  Geometry g;
+  g.lhs_rows = round_up(nrows, rowalign);
+  g.rhs_rows = 0;
+  g.cols = round_up(ncols, colalign);
+  g.lhs_block = rowalign;
+  g.rhs_block = 0;
+  return alloc_context(nrows, ncols, 0, nbits, 1, issigned, 0, g, out, "gbs_matrix_alloc");
+}
+
+}  // extern "C"
+
+namespace gbs {
+namespace {
+
+int alloc_context(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB, const Geometry &geo,
+                  gbs_ctx **out, const char *who) {
+  const std::string w(who);
+  if (!out) return fail(GBS_EINVAL, w + ": out is NULL");
   *out = nullptr;
   if (wA < 1 || wA > (uint64_t)kMaxBits || wB < 1 || wB > (uint64_t)kMaxBits)
-    return fail(GBS_EINVAL, "gbs_ctx_alloc: bit widths must be in [1, 8], got " + std::to_string(wA) +
-                                " and " + std::to_string(wB));
-  if (M > (1ull << 31) || N > (1ull << 31) || K > (1ull << 31) || M * N > (1ull << 40))
-    return fail(GBS_EINVAL, "gbs_ctx_alloc: shape too large");
+    return fail(GBS_EINVAL, w + ": bit widths must be in [1, 8], got " + std::to_string(wA) + " and " +
+                                std::to_string(wB));
+  if (M > (1ull << 31) || N > (1ull << 31) || K > (1ull << 31) || M * N > (1ull << 40) ||
+      geo.lhs_rows > (1ull << 32) || geo.rhs_rows > (1ull << 32))
+    return fail(GBS_EINVAL, w + ": shape too large");
   gbs_ctx *c = new gbs_ctx();
   if (cudaGetDevice(&c->device) != cudaSuccess) {
     delete c;
-    return cuda_fail(cudaGetLastError(), "gbs_ctx_alloc: no CUDA device");
+    return cuda_fail(cudaGetLastError(), (w + ": no CUDA device").c_str());
   }
-  auto init = [&](Mat &m, uint64_t bits, uint64_t rows, int sgn) {
+  auto init = [&](Mat &m, uint64_t bits, uint64_t rows, uint64_t rows_a, int sgn) {
     m.nbits = bits;
     m.nrows = rows;
     m.ncols = K;
     m.issigned = sgn ? 1 : 0;
-    m.nrows_a = round_up(rows, kRowAlign);
-    m.ncols_a = round_up(K, kColAlign);
+    m.nrows_a = rows_a;
+    m.ncols_a = geo.cols;
+    m.drows = round_up(rows, kRowAlign);
+    m.dcols = round_up(K, kColAlign);
   };
-  init(c->lhs, wA, M, sA);
-  init(c->rhs, wB, N, sB);
-  c->lhsBlock = c->lhs.nrows_a ? kRowAlign : 0;
-  c->rhsBlock = c->rhs.nrows_a ? kRowAlign : 0;
+  init(c->lhs, wA, M, geo.lhs_rows, sA);
+  init(c->rhs, wB, N, geo.rhs_rows, sB);
+  c->lhsBlock = geo.lhs_block;
+  c->rhsBlock = geo.rhs_block;
   cudaError_t e = cudaSuccess;
   const char *what = "";
   if (e == cudaSuccess) { what = "lhs planes"; e = dev_alloc((void **)&c->lhs.planes, c->lhs.words() * 8); }
@@ -236,7 +339,7 @@ int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, 
     cudaGetLastError();
     free_ctx_buffers(c);
     delete c;
-    return fail(GBS_ENOMEM, std::string("gbs_ctx_alloc: device allocation failed (") + what + ")");
+    return fail(GBS_ENOMEM, w + ": device allocation failed (" + what + ")");
   }
   // Planes start zeroed so that a context is well defined even before import.
   cudaMemset(c->lhs.planes, 0, c->lhs.words() * 8);
@@ -245,11 +348,16 @@ int gbs_ctx_alloc(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, 
   if (e != cudaSuccess) {
     free_ctx_buffers(c);
     delete c;
-    return cuda_fail(e, "gbs_ctx_alloc");
+    return cuda_fail(e, who);
   }
   *out = c;
   return GBS_OK;
 }
+
+}  // namespace
+}  // namespace gbs
+
+extern "C" {
 
 int gbs_ctx_allocate(uint64_t M, uint64_t K, uint64_t N, uint64_t wA, uint64_t wB, int sA, int sB,
                      gbs_ctx **out) {
@@ -620,7 +728,8 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
     ke = launch_gemm_tc_hbm(c, s, variant);
   } else if (pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM) {
     ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC_SMEM, variant);
-  } else if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor)) {
+  } else if (pipe == GBS_PIPE_BMMA && bmma_supported(sh.wa, sh.wb, e.use_xor) && sh.wpr % 2 == 0) {
+    // (b1 MMA tiles load 16-byte pieces of plane rows: an odd word count runs on the CUDA cores)
     if (e.use_xor) {
       // ncols - 2*popc(a^b) = 4*popc(a&b) - rsA - rsB - ncols, rs = bipolar row sums (2*popc - ncols)
       e.use_xor = 0;

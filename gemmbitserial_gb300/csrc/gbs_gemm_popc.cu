@@ -31,6 +31,12 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool pr
   int sz = pred ? 16 : 0;  // src-size 0 zero-fills the destination
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
 }
+// 8-byte piece: rows of an odd word count start only 8-byte aligned
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem, bool pred) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  int sz = pred ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
@@ -67,6 +73,23 @@ __device__ __forceinline__ void popc_tile(const TileArgs &g, uint64_t m0, uint64
 
   auto load_stage = [&](int st, uint64_t k0) {
     uint64_t *s = smem + st * stage_words;
+    if (wpr & 1) {  // the reference's 64-bit column padding can leave an odd word count: 8-byte pieces
+      const int a_pieces = wa * BM * KC, all = a_pieces + wb * BN * KC;
+      for (int idx = tid; idx < all; idx += NT) {
+        const bool isA = idx < a_pieces;
+        const int li = isA ? idx : idx - a_pieces;
+        const int rows = isA ? BM : BN;
+        const int plane = li / (rows * KC), rem = li % (rows * KC);
+        const int row = rem / KC, p = rem % KC;
+        const uint64_t k = k0 + p;
+        const uint64_t grow = (isA ? m0 : n0) + row;
+        const uint64_t *base = isA ? g.A + plane * g.a_plane : g.B + plane * g.b_plane;
+        uint64_t *dst = s + (isA ? plane * BM : wa * BM + plane * BN) * LDW + row * LDW + p;
+        const bool ok = k < wpr && grow < (isA ? g.a_rows : g.b_rows);
+        cp_async8(dst, ok ? base + grow * wpr + k : base, ok);
+      }
+      return;
+    }
     constexpr int per_row = KC / 2;  // 16-byte pieces per row
     const int a_pieces = wa * BM * per_row, all = a_pieces + wb * BN * per_row;
     for (int idx = tid; idx < all; idx += NT) {

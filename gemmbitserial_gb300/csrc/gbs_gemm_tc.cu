@@ -1330,11 +1330,14 @@ bool tc_encoder_available() { return encode_fn() != nullptr; }
 // A tensor-core pipe is exact for a context when every partial sum stays an
 // integer below 2^24 in fp32 and each operand's values fit e4m3 exactly (at
 // most 4 bits).  The shared-memory variants also need every plane of a stage
-// in their operand ring: at most 5 planes in total.
+// in their operand ring (at most 5 planes in total) and rows of whole 128-bit
+// stages (an even number of plane words).
 bool tc_exact(const gbs_ctx *c, int pipe) {
   const Mat &A = c->lhs, &B = c->rhs;
   if (A.nbits > 4 || B.nbits > 4 || A.nrows == 0 || B.nrows == 0 || A.ncols == 0) return false;
   if ((pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM) && A.nbits + B.nbits > 5) return false;
+  // the shared-memory variants load the planes in 2-word (128-bit) stages by TMA: rows of an even word count
+  if ((pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM) && (A.wpr() & 1)) return false;
   if ((double)A.ncols * (double)max_abs(A) * (double)max_abs(B) >= 16777216.0) return false;
   if (A.nrows_a * A.nbits > (1ull << 31) || B.nrows_a * B.nbits > (1ull << 31) || A.ncols_a >= (1ull << 31))
     return false;
@@ -1390,9 +1393,9 @@ cudaError_t launch_gemm_tc(gbs_ctx *c, cudaStream_t s, bool digits, int bn_req) 
 
 namespace {
 
-// Tensor map over a digit matrix: 2-D u8 [nrows_a][ncols_a], box 128 x 128, 128-byte swizzle.
+// Tensor map over a digit matrix ([drows][dcols] in 16-row blocks), box_rows x 128 digits, 128-byte swizzle.
 bool make_digit_map(CUtensorMap *map, const uint8_t *digits, const Mat &m, uint32_t box_rows = 128) {
-  return tc_map_u8(map, digits, m.ncols_a, m.nrows_a, box_rows);
+  return tc_map_u8(map, digits, m.dcols, m.drows, box_rows);
 }
 
 cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
@@ -1652,7 +1655,7 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   a.C = result_ptr(c);
   a.M = c->lhs.nrows;
   a.N = c->rhs.nrows;
-  a.nstages = (uint32_t)(c->lhs.ncols_a / 128);
+  a.nstages = (uint32_t)(c->lhs.dcols / 128);
   if (bn_req < 0 && (a.M < 256 || a.N < 256)) {
     // a side of fewer than 256 rows: the persistent kernel over a one-problem
     // plan (larger side as the MMA's 128-row operand, MMA N down to 16)

@@ -252,7 +252,7 @@ __device__ __forceinline__ void expand_chunk(const ExpandJob &j, uint32_t r, uin
     const uint32_t c0 = col0 + 4 * n;
     if (c0 + 4 > j.K) q[n] &= c0 >= j.K ? 0u : (0xFFFFFFFFu >> (8 * (4 - (j.K - c0))));
   }
-  *reinterpret_cast<uint4 *>(j.digits + digit_offset(r, col0, j.ncols_a)) = make_uint4(q[0], q[1], q[2], q[3]);
+  *reinterpret_cast<uint4 *>(j.digits + digit_offset(r, col0, j.dcols)) = make_uint4(q[0], q[1], q[2], q[3]);
 }
 
 __device__ __forceinline__ void expand_thread(const ExpandJob &j, uint64_t local) {
@@ -318,7 +318,7 @@ ExpandJob make_expand_job(const Mat &m, uint8_t *digits) {
   j.digits = digits;
   j.nrows_a = m.nrows_a;
   j.wpr = m.wpr();
-  j.ncols_a = m.ncols_a;
+  j.dcols = m.dcols;
   j.nrows = (uint32_t)m.nrows;
   j.K = (uint32_t)m.ncols;
   j.chunks = (uint32_t)((m.ncols + 15) / 16);
@@ -335,12 +335,12 @@ cudaError_t launch_expand(const ExpandJob &job, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// Digit matrix [nrows_a][ncols_a] of one side, allocated zeroed on first use
+// Digit matrix [drows][dcols] of one side, allocated zeroed on first use
 // (synchronously: kernels on any stream may write it right after).
 cudaError_t ensure_digit_buffer(gbs_ctx *c, int side) {
   if (c->digits[side]) return cudaSuccess;
   const Mat &m = side ? c->rhs : c->lhs;
-  const size_t bytes = std::max<size_t>(m.nrows_a * m.ncols_a, 16);
+  const size_t bytes = std::max<size_t>(m.drows * m.dcols, 16);
   cudaError_t e = dev_alloc((void **)&c->digits[side], bytes);
   if (e == cudaSuccess) e = cudaMemset(c->digits[side], 0, bytes);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -396,13 +396,13 @@ int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
     P.swap = L.nrows < R.nrows ? 1u : 0u;
     const Mat &MA = P.swap ? R : L, &MB = P.swap ? L : R;
     const uint8_t *da = c->digits[P.swap ? 1 : 0], *db = c->digits[P.swap ? 0 : 1];
-    P.a_rows = (uint32_t)MA.nrows_a;
-    P.b_rows = (uint32_t)MB.nrows_a;
+    P.a_rows = (uint32_t)MA.drows;
+    P.b_rows = (uint32_t)MB.drows;
     P.nk = (uint32_t)((L.ncols + 127) / 128);
     P.bn = (uint32_t)std::min<uint64_t>(256, (MB.nrows + 15) / 16 * 16);
     P.idesc = (1u << 4) | ((P.bn >> 3) << 17) | ((128u >> 4) << 24);
     CUtensorMap m2[2];
-    if (!tc_map_u8(&m2[0], da, MA.ncols_a, MA.nrows_a, 128) || !tc_map_u8(&m2[1], db, MB.ncols_a, MB.nrows_a, P.bn))
+    if (!tc_map_u8(&m2[0], da, MA.dcols, MA.drows, 128) || !tc_map_u8(&m2[1], db, MB.dcols, MB.drows, P.bn))
       return fail(GBS_EUNSUPPORTED, "tensor-core plan: tensor map encoding failed");
     maps.push_back(m2[0]);
     maps.push_back(m2[1]);

@@ -114,6 +114,7 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
       j.dtype = dt;
       j.vec = (dt == GBS_I8 || dt == GBS_U8) && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0;
       j.segs = (uint32_t)pack_segs_per_row(m.wpr());
+      j.dcols = m.dcols;
       if (g->is_tc[p]) {  // tensor-core problem: the import writes its digit matrices too
         j.digits = g->ctxs[p]->digits[side];
         tc_digit_table(m, j.dtab);

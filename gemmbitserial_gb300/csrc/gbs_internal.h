@@ -12,8 +12,11 @@ namespace gbs {
 
 struct AdjPlan;  // workspace of the tensor-core adjoint (gbs_adjoint_tc.cu)
 
-constexpr uint64_t kRowAlign = 256;  // device row padding (rows of a plane): a multiple of every tile's row count
-constexpr uint64_t kColAlign = 256;  // device column padding (bits of a row)
+// Padding of the e4m3 digit matrices (the tensor-core operands): rows to a
+// multiple of every tile's row count, columns to whole 256-digit stages.  The
+// bit planes themselves keep the reference's padding (gbs_ctx_alloc).
+constexpr uint64_t kRowAlign = 256;
+constexpr uint64_t kColAlign = 256;
 constexpr int kMaxBits = 8;
 
 // e4m3 digit matrices (the tensor-core pipe's operands) are stored in 16-row
@@ -26,9 +29,14 @@ __host__ __device__ inline uint64_t digit_offset(uint64_t r, uint64_t col, uint6
   return ((r >> 4) * (ncols_a >> 7) + (col >> 7)) * 2048 + ((r & 15) << 7) + (col & 127);
 }
 
-// One bit-serial matrix on the device: planes [nbits][nrows_a][wpr] of u64.
+// One bit-serial matrix on the device: planes [nbits][nrows_a][wpr] of u64,
+// with the reference's nrows_a and ncols_a (BitSerialMatrix, gemmbitserial.hpp:
+// 24-50): rows padded to the context's cache block, columns to 64 bits (256
+// for matrix-vector contexts).  drows x dcols is the geometry of the
+// matrix's e4m3 digit matrix (rows and columns padded to 256).
 struct Mat {
   uint64_t nbits = 0, nrows = 0, ncols = 0, nrows_a = 0, ncols_a = 0;
+  uint64_t drows = 0, dcols = 0;
   int issigned = 0;
   uint64_t *planes = nullptr;
   bool imported = false;
@@ -87,6 +95,7 @@ struct PackJob {
   int32_t *rowsum;
   uint8_t *digits;
   uint64_t nrows, ncols, nrows_a, wpr, warp0;
+  uint64_t dcols;  // digit-matrix columns (a multiple of 256)
   int nbits, issigned, dtype, vec;
   uint32_t segs;  // 512-column segments per row
   uint32_t dtab[4];
@@ -114,7 +123,7 @@ struct TcgTile {
 struct ExpandJob {
   const uint64_t *planes;
   uint8_t *digits;
-  uint64_t nrows_a, wpr, ncols_a;
+  uint64_t nrows_a, wpr, dcols;  // plane rows and words per row; digit-matrix columns
   uint64_t thread0;  // first global thread of this job (16 digits per thread)
   uint32_t nrows, K, chunks, nbits;
   uint32_t tab[4];   // e4m3 byte of every plane code, 4 per word
@@ -172,7 +181,7 @@ struct gbs_ctx {
   alignas(64) unsigned char tc_map_a[128];
   alignas(64) unsigned char tc_map_b[128];
   bool tc_maps_ready = false;
-  // e4m3 digit matrices [nrows_a][ncols_a] of both operands (the tensor-core
+  // e4m3 digit matrices [drows][dcols] of both operands (the tensor-core
   // pipe's operands), built from the planes on first use after each import
   uint8_t *digits[2] = {nullptr, nullptr};
   bool digits_valid[2] = {false, false};

@@ -90,6 +90,8 @@ extern "C" int gbs_gemm_noalloc(const void *lhs, int lhs_dtype, const void *rhs,
     m.issigned = sgn ? 1 : 0;
     m.nrows_a = round_up(rows, kRowAlign);
     m.ncols_a = round_up(K, kColAlign);
+    m.drows = m.nrows_a;
+    m.dcols = m.ncols_a;
     m.imported = true;
   };
   init(c.lhs, lhsBits, M, lhsSigned);

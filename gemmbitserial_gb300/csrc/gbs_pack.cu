@@ -118,10 +118,11 @@ __device__ __forceinline__ uint32_t digits4(uint32_t x, int nbits, uint4 tab) {
   return (lo & ~m) | (hi & m);
 }
 
-// The lane's 32 digits of padded row r (0 past nrows and past ncols) into the
-// digit matrix (64 * wpr columns, 16-row blocks: digit_offset).
+// The lane's 32 digits of row r < nrows (0 past ncols) into the digit matrix
+// (dcols columns, 16-row blocks: digit_offset).  Digit rows past nrows and
+// columns past the planes' padded width stay as allocated: zero.
 __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int nbits, uint64_t nrows,
-                                               uint64_t ncols, uint64_t wpr, uint4 tab, uint64_t r, uint64_t col0,
+                                               uint64_t ncols, uint64_t dcols, uint4 tab, uint64_t r, uint64_t col0,
                                                const uint32_t (&q)[8]) {
   uint32_t d[8];
 #pragma unroll
@@ -133,7 +134,7 @@ __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int
       if (c + 4 > ncols) d[i] &= c >= ncols ? 0u : (0xFFFFFFFFu >> (8 * (4 - (ncols - c))));
     }
   }
-  uint4 *dst = reinterpret_cast<uint4 *>(digits + digit_offset(r, col0, wpr * 64));
+  uint4 *dst = reinterpret_cast<uint4 *>(digits + digit_offset(r, col0, dcols));
   dst[0] = make_uint4(d[0], d[1], d[2], d[3]);
   dst[1] = make_uint4(d[4], d[5], d[6], d[7]);
 }
@@ -142,14 +143,14 @@ __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int
 __device__ __forceinline__ void pack_unit(const void *__restrict__ src, int dtype, int bipolar, int issigned,
                                           int nbits,
                                           uint64_t nrows, uint64_t ncols, uint64_t nrows_a, uint64_t wpr, int vec,
-                                          uint64_t *__restrict__ planes, uint8_t *__restrict__ digits, uint4 dtab,
-                                          uint64_t r, uint64_t seg, int lane) {
+                                          uint64_t *__restrict__ planes, uint8_t *__restrict__ digits,
+                                          uint64_t dcols, uint4 dtab, uint64_t r, uint64_t seg, int lane) {
   const uint64_t col0 = seg * kSegCols + (uint64_t)lane * 32;
   if (col0 >= wpr * 64) return;  // past the padded row
   uint32_t q[8];
   load_codes32(src, dtype, bipolar, issigned, nbits, nrows, ncols, vec, r, col0, q);
   emit_planes32(nbits, nrows_a, wpr, planes, r, col0, q);
-  if (digits) write_digits32(digits, nbits, nrows, ncols, wpr, dtab, r, col0, q);
+  if (digits && r < nrows) write_digits32(digits, nbits, nrows, ncols, dcols, dtab, r, col0, q);
 }
 
 // Row-major pack of padded rows [row0, row0 + nrows_launch).  With digits
@@ -160,11 +161,11 @@ __global__ void __launch_bounds__(256) pack_rowmajor(const void *__restrict__ sr
                                                      uint64_t nrows_a, uint64_t wpr, int vec,
                                                      uint64_t *__restrict__ planes, uint64_t row0,
                                                      uint64_t nrows_launch, uint8_t *__restrict__ digits,
-                                                     uint4 dtab) {
+                                                     uint64_t dcols, uint4 dtab) {
   const uint64_t segs = segs_per_row(wpr);
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= nrows_launch * segs) return;  // warp-uniform
-  pack_unit(src, dtype, bipolar, issigned, nbits, nrows, ncols, nrows_a, wpr, vec, planes, digits, dtab,
+  pack_unit(src, dtype, bipolar, issigned, nbits, nrows, ncols, nrows_a, wpr, vec, planes, digits, dcols, dtab,
             row0 + warp / segs,
             warp % segs, threadIdx.x & 31);
 }
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(256) pack_quantize_kernel(const T *__restrict_
                                                             int nthres, int nbits, uint64_t nrows, uint64_t ncols,
                                                             uint64_t nrows_a, uint64_t wpr, int col_major,
                                                             uint64_t *__restrict__ planes,
-                                                            uint8_t *__restrict__ digits, uint4 dtab) {
+                                                            uint8_t *__restrict__ digits, uint64_t dcols, uint4 dtab) {
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   uint64_t r, col0;
@@ -212,9 +213,10 @@ __global__ void __launch_bounds__(256) pack_quantize_kernel(const T *__restrict_
     col0 = (warp % segs) * kSegCols + (uint64_t)lane * 32;
   } else {
     const uint64_t cblocks = wpr * 2;
-    if (warp >= (nrows_a / 32) * cblocks) return;
+    if (warp >= ((nrows_a + 31) / 32) * cblocks) return;
     r = (warp / cblocks) * 32 + lane;
     col0 = (warp % cblocks) * 32;
+    if (r >= nrows_a) return;  // lanes past the padded rows (no warp-wide step follows)
   }
   if (col0 >= wpr * 64) return;
   uint32_t q[8];
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(256) pack_quantize_kernel(const T *__restrict_
     }
   }
   emit_planes32(nbits, nrows_a, wpr, planes, r, col0, q);
-  if (digits) write_digits32(digits, nbits, nrows, ncols, wpr, dtab, r, col0, q);
+  if (digits && r < nrows) write_digits32(digits, nbits, nrows, ncols, dcols, dtab, r, col0, q);
 }
 
 // Index of the job owning global warp w: the last job with warp0 <= w.
@@ -298,9 +300,9 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
       const uint64_t col0 = sc * kSegCols + (uint64_t)lane * 32;
       if (col0 < J.wpr * 64) {
         emit_planes32(J.nbits, J.nrows_a, J.wpr, J.planes, rc, col0, q);
-        if (J.digits) {
+        if (J.digits && rc < J.nrows) {
           const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
-          write_digits32(J.digits, J.nbits, J.nrows, J.ncols, J.wpr, tab, rc, col0, q);
+          write_digits32(J.digits, J.nbits, J.nrows, J.ncols, J.dcols, tab, rc, col0, q);
         }
       }
       if (w + 1 < last) {
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ sr
                                                      int issigned, int nbits, uint64_t nrows, uint64_t ncols,
                                                      uint64_t nrows_a, uint64_t wpr,
                                                      uint64_t *__restrict__ planes) {
-  const uint64_t rgroups = nrows_a / 32;
+  const uint64_t rgroups = (nrows_a + 31) / 32;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= rgroups * wpr) return;  // warp-uniform
@@ -355,6 +357,7 @@ __global__ void __launch_bounds__(256) pack_colmajor(const void *__restrict__ sr
   }
   const uint64_t plane_words = nrows_a * wpr;
   const uint64_t r = r0 + lane;
+  if (r >= nrows_a) return;  // the last group's lanes past the padded rows
 #pragma unroll
   for (int b = 0; b < kMaxBits; b++)
     if (b < nbits) planes[b * plane_words + r * wpr + w] = (uint64_t)lo[b] | ((uint64_t)hi[b] << 32);
@@ -435,7 +438,7 @@ cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t 
   const uint4 tab = dtab ? make_uint4(dtab[0], dtab[1], dtab[2], dtab[3]) : make_uint4(0u, 0u, 0u, 0u);
   pack_rowmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, m.issigned, (int)m.nbits, m.nrows, m.ncols,
                                                           m.nrows_a, m.wpr(), vec, m.planes, r0, r1 - r0,
-                                                          digits, tab);
+                                                          digits, m.dcols, tab);
   count_launch();
   return cudaGetLastError();
 }
@@ -443,12 +446,13 @@ cudaError_t launch_pack_rows(const Mat &m, const void *src, int dtype, uint64_t 
 cudaError_t launch_pack_quantize(const Mat &m, const void *src, const void *thr, int nthres, int dtype,
                                  int col_major, uint8_t *digits, const uint32_t *dtab, cudaStream_t s) {
   if (m.nrows_a == 0 || m.wpr() == 0) return cudaSuccess;
-  const uint64_t warps = col_major ? (m.nrows_a / 32) * m.wpr() * 2 : m.nrows_a * segs_per_row(m.wpr());
+  const uint64_t warps = col_major ? ((m.nrows_a + 31) / 32) * m.wpr() * 2 : m.nrows_a * segs_per_row(m.wpr());
   const unsigned blocks = blocks_for(warps * 32, 256);
   const uint4 tab = dtab ? make_uint4(dtab[0], dtab[1], dtab[2], dtab[3]) : make_uint4(0u, 0u, 0u, 0u);
 #define GBS_QLAUNCH(T)                                                                                              \
   pack_quantize_kernel<T><<<blocks, 256, 0, s>>>((const T *)src, (const T *)thr, nthres, (int)m.nbits, m.nrows,      \
-                                                 m.ncols, m.nrows_a, m.wpr(), col_major, m.planes, digits, tab)
+                                                 m.ncols, m.nrows_a, m.wpr(), col_major, m.planes, digits, m.dcols, \
+                                                 tab)
   switch (dtype) {
     case GBS_I8: GBS_QLAUNCH(int8_t); break;
     case GBS_U8: GBS_QLAUNCH(uint8_t); break;
@@ -467,7 +471,7 @@ cudaError_t launch_pack(const Mat &m, const void *src, int dtype, int col_major,
   if (!col_major) {
     return launch_pack_rows(m, src, dtype, 0, m.nrows_a, nullptr, nullptr, s);
   } else {
-    const uint64_t warps = (m.nrows_a / 32) * m.wpr();
+    const uint64_t warps = ((m.nrows_a + 31) / 32) * m.wpr();
     pack_colmajor<<<blocks_for(warps * 32, 256), 256, 0, s>>>(src, dtype, bip, m.issigned, (int)m.nbits, m.nrows, m.ncols,
                                                             m.nrows_a, m.wpr(), m.planes);
   }

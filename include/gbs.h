@@ -12,11 +12,11 @@
  * reference's class API on top of these calls.
  *
  * Matrix storage on the device keeps the reference's bit-serial layout
- * (gemmbitserial.hpp:50): 64-bit words, [nbits][nrows_a][ncols_a/64], column c
- * of row r in plane b at word c>>6, bit c&63, all padding zero.  The device
- * pads rows to a multiple of 256 and columns to a multiple of 256 (the
- * reference pads columns to 64, or to 256 for matrix-vector contexts, and
- * rows to its cache block); results never depend on padding.
+ * (gemmbitserial.hpp:50) and padding: 64-bit words, [nbits][nrows_a][ncols_a/64],
+ * column c of row r in plane b at word c>>6, bit c&63, all padding zero; a
+ * context pads columns to 64 bits (256 for matrix-vector contexts) and rows to
+ * the reference's cache block (gbs_ctx_dims).  The tensor-core pipe keeps its
+ * e4m3 digit copies of the operands in a separate, 256-padded layout.
  */
 #ifndef GBS_H_
 #define GBS_H_
@@ -81,7 +81,7 @@ typedef struct {
 
 typedef struct {
   gbs_matrix_info lhs, rhs;
-  uint64_t lhsBlock, rhsBlock; /* device tile rows (lhs, rhs) */
+  uint64_t lhsBlock, rhsBlock; /* the reference's cache blocks (rows of lhs, rhs) */
   int32_t *res;                /* DEVICE pointer, rhs.nrows x lhs.nrows, transposed layout: the
                                   last gbs_gemm's result (not written by gbs_gemm_to into a caller
                                   buffer) */
@@ -95,6 +95,20 @@ typedef struct {
  * the current CUDA device.  M, N or K may be 0 (empty result). */
 GBS_API int gbs_ctx_alloc(uint64_t lhsRows, uint64_t depth, uint64_t rhsRows, uint64_t lhsBits,
                   uint64_t rhsBits, int lhsSigned, int rhsSigned, gbs_ctx **out);
+
+/* The padding allocGEMMContext gives a context, without allocating:
+ * dims = {lhs.nrows_a, rhs.nrows_a, lhs.ncols_a, rhs.ncols_a, lhsBlock,
+ * rhsBlock}, as the reference computes them (arch-generic.hpp:78-100,
+ * gemmbitserial.hpp:343-377, 415-452): columns to 64 bits (256 when N == 1),
+ * rows to the cache blocks.  gbs_ctx_alloc allocates exactly this geometry. */
+GBS_API int gbs_ctx_dims(uint64_t lhsRows, uint64_t depth, uint64_t rhsRows, uint64_t *dims);
+
+/* Replaces BitSerialMatrix::alloc (gemmbitserial.hpp:24-35): a context whose
+ * lhs is one nbits x nrows x ncols matrix with rows padded to rowalign (>= 1)
+ * and columns to colalign bits (a positive multiple of 64); its rhs is empty.
+ * Import, export, get/set and row sums work on it as on a context's lhs. */
+GBS_API int gbs_matrix_alloc(uint64_t nbits, uint64_t nrows, uint64_t ncols, int issigned, uint64_t rowalign,
+                             uint64_t colalign, gbs_ctx **out);
 
 /* Alias of gbs_ctx_alloc under the name the reference README uses
  * (README.md:15, "allocateGEMMContext"). */

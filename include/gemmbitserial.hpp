@@ -49,14 +49,12 @@ class BitSerialMatrix {
   gbs_ctx *ctx_ = nullptr;  // owning context (shared by copies)
   int side_ = GBS_LHS;
 
-  // BitSerialMatrix::alloc (reference gemmbitserial.hpp:24-35).  The device
-  // chooses its own padding, so rowalign/colalign are accepted and ignored.
+  // BitSerialMatrix::alloc (reference gemmbitserial.hpp:24-35): rows padded
+  // to rowalign, columns to colalign bits (a multiple of 64), on the device.
   static BitSerialMatrix alloc(uint64_t nbits, uint64_t nrows, uint64_t ncols, bool issigned,
                                uint64_t rowalign = 1, uint64_t colalign = 64) {
-    (void)rowalign;
-    (void)colalign;
     gbs_ctx *c = nullptr;
-    detail::check(gbs_ctx_alloc(nrows, ncols, 0, nbits, 1, issigned ? 1 : 0, 0, &c));
+    detail::check(gbs_matrix_alloc(nbits, nrows, ncols, issigned ? 1 : 0, rowalign, colalign, &c));
     try {
       return from_ctx(c, GBS_LHS);
     } catch (...) {

@@ -64,6 +64,23 @@ int main() {
         }
     failed += report("conversions", ok, total);
   }
+  {  // BitSerialMatrix::alloc pads as the reference does: rows to rowalign, columns to colalign
+    int ok = 0, total = 0;
+    for (uint64_t ra : {1, 2, 7, 64})
+      for (uint64_t ca : {64, 128, 256}) {
+        BitSerialMatrix m = BitSerialMatrix::alloc(3, 37, 300, false, ra, ca);
+        ok += m.nrows_a == (37 + ra - 1) / ra * ra && m.ncols_a == (300 + ca - 1) / ca * ca &&
+              m.wordsPerRow() == m.ncols_a / 64;
+        total++;
+        BitSerialMatrix::dealloc(m);
+      }
+    GEMMContext g = allocGEMMContext(2048, 4096, 2048, 3, 2, false, true);  // the reference: 2070 / 4096 / 30
+    ok += g.lhs.nrows_a == 2070 && g.rhs.nrows_a == 2070 && g.lhs.ncols_a == 4096 && g.lhsBlock == 30 &&
+          g.rhsBlock == 30;
+    total++;
+    deallocGEMMContext(g);
+    failed += report("padding", ok, total);
+  }
   {  // sumRows on a copy of ctx.lhs, all d sums
     int ok = 0, total = 0;
     for (int b : {1, 2, 3, 4})

@@ -59,3 +59,23 @@ def test_python_api_fails_loudly_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(_capi, "lib_path", lambda: str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError, match="not built"):
         _capi.load()
+
+
+def test_context_padding_is_the_references(gbs_lib):
+    """gbs_ctx_dims (host arithmetic, no device) gives the reference's lhs/rhs nrows_a, ncols_a and
+    cache blocks for every golden vector and full-size workload, as the compiled reference recorded."""
+    import json
+
+    from gemmbitserial_gb300 import datagen
+    gold = os.path.join(ROOT, "tests", "golden")
+    cases = [((v["M"], v["K"], v["N"]), v["ref_dims"]) for v in json.load(open(os.path.join(gold, "ref_vectors.json")))["gemm"]]
+    cfg = json.load(open(os.path.join(gold, "ref_configs.json")))
+    cases += [((M, K, N), cfg[name]["dims"]) for name, (M, K, N, _a, _b) in datagen.WORKLOADS.items()]
+    for (M, K, N), want in cases:
+        out = (C.c_uint64 * 6)()
+        assert gbs_lib.gbs_ctx_dims(M, K, N, out) == 0
+        assert list(out) == want, (M, K, N)
+    # degenerate sides pad to nothing; matrix-vector depth pads to 256 bits
+    out = (C.c_uint64 * 6)()
+    assert gbs_lib.gbs_ctx_dims(0, 100, 5, out) == 0 and out[0] == 0 and out[2] == 128
+    assert gbs_lib.gbs_ctx_dims(10, 100, 1, out) == 0 and out[2] == 256

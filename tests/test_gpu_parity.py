@@ -93,7 +93,7 @@ def test_rowsums_and_export(r):
 
 
 def test_packed_planes_match_oracle():
-    """Device planes hold the reference layout (plus zero padding)."""
+    """Device planes hold the reference layout with the reference's padding."""
     rng = np.random.default_rng(5)
     for dt in (np.int8, np.uint8, np.int16, np.int32):
         for cm in (False, True):
@@ -107,9 +107,9 @@ def test_packed_planes_match_oracle():
                     oc.import_(0, Xin, cm)
                     dev = ctx.lhs.planes()
                     ref = oc.planes(0)
-                    wpr = ref.shape[2]
-                    assert np.array_equal(dev[:, :M, :wpr], ref[:, :M, :]), (dt, cm, M, K)
-                    assert not dev[:, M:, :].any() and not dev[:, :, wpr:].any()
+                    # the reference's geometry and padding, word for word (padding zero in both)
+                    assert dev.shape == ref.shape, (dt, cm, M, K)
+                    assert np.array_equal(dev, ref), (dt, cm, M, K)
                 finally:
                     deallocGEMMContext(ctx)
                     oc.close()
@@ -230,3 +230,25 @@ def test_launches_are_counted(lib):
     before = lib.gbs_debug_launch_count()
     gpu_gemm(np.ones((4, 64), np.int8), np.ones((4, 64), np.int8), 1, 1, 0, 0)
     assert lib.gbs_debug_launch_count() >= before + 3  # two packs and one forward kernel
+
+
+def test_context_geometry_is_the_references():
+    """Every golden vector's context reports the reference's nrows_a, ncols_a, lhsBlock and rhsBlock
+    (arch-generic.hpp:78-100, gemmbitserial.hpp:415-452), as recorded by the compiled reference."""
+    from gemmbitserial_gb300 import _capi
+    lib = _capi.load()
+    seen = set()
+    for v in VEC["gemm"]:
+        key = (v["M"], v["K"], v["N"])
+        if key in seen:
+            continue
+        seen.add(key)
+        ctx = allocGEMMContext(v["M"], v["K"], v["N"], v["wA"], v["wB"], v["sA"], v["sB"])
+        try:
+            info = _capi.CtxInfo()
+            _capi.check(lib.gbs_ctx_get_info(ctx._h, C.byref(info)))
+            got = [info.lhs.nrows_a, info.rhs.nrows_a, info.lhs.ncols_a, info.rhs.ncols_a, info.lhsBlock, info.rhsBlock]
+            assert got == v["ref_dims"], key
+            assert ctx.lhs.planes().shape == (v["wA"], v["ref_dims"][0], v["ref_dims"][2] // 64)
+        finally:
+            deallocGEMMContext(ctx)

@@ -40,7 +40,11 @@ def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True, pipe=_capi.GBS_PIPE_TC):
             _capi.check(_capi.load().gbs_set_variant(ctx._h, variant))
         ctx.set_pipe(pipe)
         if expect_tc:
-            assert ctx.pipe == pipe, "tensor-core pipe not applicable"
+            wpr = -(-K // 64) if N != 1 else -(-K // 256) * 4  # the reference's words per plane row
+            if pipe in (_capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS) and wpr % 2:
+                assert ctx.pipe == _capi.GBS_PIPE_POPC, "odd word count: the shared-memory variants decline"
+            else:
+                assert ctx.pipe == pipe, "tensor-core pipe not applicable"
         ctx.lhs.importRegular(A)
         ctx.rhs.importRegular(B)
         gemmBitSerial(ctx)
@@ -120,6 +124,12 @@ def test_tc_pipe_declines_what_it_cannot_do_exactly():
         assert ctx.pipe == _capi.GBS_PIPE_POPC
         deallocGEMMContext(ctx)
     ctx = allocGEMMContext(128, 256, 128, 4, 4, False, False)
+    ctx.set_pipe(_capi.GBS_PIPE_TC_SMEM)
+    assert ctx.pipe == _capi.GBS_PIPE_POPC
+    ctx.set_pipe(_capi.GBS_PIPE_TC)
+    assert ctx.pipe == _capi.GBS_PIPE_TC
+    deallocGEMMContext(ctx)
+    ctx = allocGEMMContext(128, 320, 128, 2, 2, False, False)  # 5 plane words per row: 128-bit stages do not fit
     ctx.set_pipe(_capi.GBS_PIPE_TC_SMEM)
     assert ctx.pipe == _capi.GBS_PIPE_POPC
     ctx.set_pipe(_capi.GBS_PIPE_TC)
