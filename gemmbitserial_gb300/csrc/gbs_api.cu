@@ -127,6 +127,7 @@ void free_ctx_buffers(gbs_ctx *c) {
     delete c->plan1;
   }
   adj_plan_free(c->adj);
+  wide_plan_free(c->wide);
   if (c->sk_ws) cudaFree(c->sk_ws);
   if (c->sk_flags) cudaFree(c->sk_flags);
   if (c->digits[0]) cudaFree(c->digits[0]);
@@ -234,6 +235,7 @@ int choose_pipe(const gbs_ctx *c);
 // the CUDA cores for shapes it does not cover.
 int effective_pipe(const gbs_ctx *c) {
   const int p = c->pipe == GBS_PIPE_AUTO ? choose_pipe(c) : c->pipe;
+  if (p == GBS_PIPE_TC && tc_wide(c)) return p;  // 5-8-bit operands in parts of <= 4 bits
   if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && !tc_exact(c, p)) return GBS_PIPE_POPC;
   return p;
 }
@@ -429,7 +431,9 @@ int ensure_stage(gbs_ctx *c, int side, size_t bytes, cudaStream_t s) {
 
 // The tensor-core digit pipe will run this context's GEMM: the import then
 // writes the digit matrix too, so the GEMM needs no expansion pass.
-bool import_writes_digits(const gbs_ctx *c) { return effective_pipe(c) == GBS_PIPE_TC; }
+bool import_writes_digits(const gbs_ctx *c) {
+  return effective_pipe(c) == GBS_PIPE_TC && c->lhs.nbits <= 4 && c->rhs.nbits <= 4;  // wide operands: per part, later
+}
 
 }  // namespace
 
@@ -724,7 +728,9 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   const int variant = c->variant >= 0 ? c->variant : (c->pipe == GBS_PIPE_AUTO ? tuned_variant(c, pipe) : -1);
   sh.tile_cls = (pipe == GBS_PIPE_POPC && variant >= 0 && variant <= 2) ? variant : -1;
   cudaError_t ke;
-  if (pipe == GBS_PIPE_TC) {
+  if (pipe == GBS_PIPE_TC && tc_wide(c)) {
+    ke = launch_gemm_wide(c, s, variant);
+  } else if (pipe == GBS_PIPE_TC) {
     ke = launch_gemm_tc_hbm(c, s, variant);
   } else if (pipe == GBS_PIPE_TC_PAIRS || pipe == GBS_PIPE_TC_SMEM) {
     ke = launch_gemm_tc(c, s, pipe == GBS_PIPE_TC_SMEM, variant);

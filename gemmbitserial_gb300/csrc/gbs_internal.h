@@ -10,7 +10,8 @@
 
 namespace gbs {
 
-struct AdjPlan;  // workspace of the tensor-core adjoint (gbs_adjoint_tc.cu)
+struct AdjPlan;   // workspace of the tensor-core adjoint (gbs_adjoint_tc.cu)
+struct WidePlan;  // part sub-contexts of a context with 5-8-bit operands (gbs_wide.cu)
 
 // Padding of the e4m3 digit matrices (the tensor-core operands): rows to a
 // multiple of every tile's row count, columns to whole 256-digit stages.  The
@@ -202,6 +203,7 @@ struct gbs_ctx {
   gbs::TcgPlan *plan1 = nullptr;
   bool plan1_ready = false;
   gbs::AdjPlan *adj = nullptr;  // tensor-core adjoint workspace, built on first use
+  gbs::WidePlan *wide = nullptr;  // tensor-core parts of 5-8-bit operands, built on first use
   bool vt_valid[2] = {false, false};  // its transposed bf16 operand values match the planes
 };
 
@@ -279,6 +281,10 @@ void tcg_plan_free(TcgPlan *plan);
 cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s);
 cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s, int32_t *out0 = nullptr);
 cudaError_t ensure_digit_buffer(gbs_ctx *c, int side);
+// tensor-core pipe for 5-8-bit operands (gbs_wide.cu): operands split into parts of <= 4 bits
+bool tc_wide(const gbs_ctx *c);
+cudaError_t launch_gemm_wide(gbs_ctx *c, cudaStream_t s, int variant);
+void wide_plan_free(WidePlan *p);
 // tensor-core adjoint (gbs_adjoint_tc.cu)
 int adjoint_tc(gbs_ctx *c, const float *dC, float *dA, float *dB, cudaStream_t s);
 bool adjoint_tc_available();

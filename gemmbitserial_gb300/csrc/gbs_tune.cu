@@ -147,9 +147,10 @@ int choose_pipe(const gbs_ctx *c) {
       const int p = it->second.pipe;
       if (p == GBS_PIPE_POPC || p == GBS_PIPE_BMMA) return p;
       if ((p == GBS_PIPE_TC || p == GBS_PIPE_TC_PAIRS || p == GBS_PIPE_TC_SMEM) && tc_exact(c, p)) return p;
+      if (p == GBS_PIPE_TC && tc_wide(c)) return p;
     }
   }
-  return (tc_exact(c, GBS_PIPE_TC) && tcg_preferred(c)) ? GBS_PIPE_TC : GBS_PIPE_POPC;
+  return ((tc_exact(c, GBS_PIPE_TC) || tc_wide(c)) && tcg_preferred(c)) ? GBS_PIPE_TC : GBS_PIPE_POPC;
 }
 
 int tuned_variant(const gbs_ctx *c, int pipe) {
@@ -292,6 +293,7 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
   int nc = 0;
   for (int v = -1; v <= 2; v++) cands[nc++] = Cand{GBS_PIPE_POPC, v};  // -1: built-in tile rule
   cands[nc++] = Cand{GBS_PIPE_BMMA, -1};
+  if (tc_wide(c)) cands[nc++] = Cand{GBS_PIPE_TC, -1};  // 5-8-bit operands: part products on the digit pipe
   if (tc_exact(c, GBS_PIPE_TC)) {
     cands[nc++] = Cand{GBS_PIPE_TC, -1};  // built-in rule: SM pairs, or the persistent kernel for a side < 256
     cands[nc++] = Cand{GBS_PIPE_TC, 128};
