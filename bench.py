@@ -400,12 +400,32 @@ def measure_configs(lib, dev, stream, reps=50, warmup=5):
         lp = [C.c_int(0), C.c_int(0), C.c_int(0)]
         _capi.check(lib.gbs_debug_last_pair(ctx._h, *(C.byref(x) for x in lp)))
         deallocGEMMContext(ctx)
+        cuda_core_ms = None
+        if max(wA, wB) > 4 and pipe == _capi.GBS_PIPE_TC:  # wide operands: the CUDA-core pipe beside it
+            c2 = allocGEMMContext(M, K, N, wA, wB, sA, sB)
+            c2.set_pipe(_capi.GBS_PIPE_POPC)
+            with torch.cuda.stream(stream):
+                c2.lhs.importRegular(torch.from_numpy(A).to(dev), stream=stream)
+                c2.rhs.importRegular(torch.from_numpy(B).to(dev), stream=stream)
+                flush.zero_()
+                _capi.check(lib.gbs_gemm(c2._h, sh))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                flush.zero_()
+                e0.record(stream)
+                _capi.check(lib.gbs_gemm(c2._h, sh))
+                e1.record(stream)
+            stream.synchronize()
+            cuda_core_ms = e0.elapsed_time(e1)
+            deallocGEMMContext(c2)
         kpad = (K + 63) // 64 * 64
         packed = wA * M * kpad // 8 + wB * N * kpad // 8 + 4 * M * N
         out[name] = {"ms": round(ms, 4), "gops": round(gops(M, K, N, ms * 1e-3), 1), "pipe": names.get(pipe, pipe),
                      "tbinops": round(2.0 * M * N * kpad * wA * wB / (ms * 1e-3) / 1e12, 2),
                      "gbs_packed_bytes": round(packed / (ms * 1e-3) / 1e9, 1),
                      "tuned": tuned, "pair_kernel": pair_kernel_name(lp),
+                     **({"cuda_core_ms": round(cuda_core_ms, 4), "speedup_vs_cuda_cores": round(cuda_core_ms / ms, 1),
+                         "how": "operands split into plane parts of <= 4 bits, one digit GEMM per part pair"}
+                        if cuda_core_ms else {}),
                      "parity": "bit-exact vs reference (sha256)" if ok else "MISMATCH"}
     return out
 

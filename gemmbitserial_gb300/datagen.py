@@ -80,6 +80,8 @@ WORKLOADS = {
     "gemm_256x9216x4096_bps4": (256, 9216, 4096, (1, "b"), (4, "s")),
     # forward of the adjoint layer: 2-bit unsigned activations, bipolar weights.
     "gemm_4096x2048x2048_u2bp": (4096, 2048, 2048, (2, "u"), (1, "b")),
+    # the headline shape at 8-bit signed x 8-bit signed (wider than one e4m3 digit).
+    "gemm_2048x4096x2048_s8s8": (2048, 4096, 2048, (8, "s"), (8, "s")),
 }
 
 

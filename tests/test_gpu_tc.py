@@ -41,8 +41,9 @@ def tc_gemm(A, B, wA, wB, sA, sB, expect_tc=True, pipe=_capi.GBS_PIPE_TC):
         ctx.set_pipe(pipe)
         if expect_tc:
             wpr = -(-K // 64) if N != 1 else -(-K // 256) * 4  # the reference's words per plane row
-            if pipe in (_capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS) and wpr % 2:
-                assert ctx.pipe == _capi.GBS_PIPE_POPC, "odd word count: the shared-memory variants decline"
+            if pipe in (_capi.GBS_PIPE_TC_SMEM, _capi.GBS_PIPE_TC_PAIRS) and (wpr % 2 or max(wA, wB) > 4):
+                # odd word counts and operands wider than one digit: the shared-memory variants decline
+                assert ctx.pipe == _capi.GBS_PIPE_POPC
             else:
                 assert ctx.pipe == pipe, "tensor-core pipe not applicable"
         ctx.lhs.importRegular(A)
