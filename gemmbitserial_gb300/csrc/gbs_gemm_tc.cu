@@ -1200,8 +1200,9 @@ __global__ void __launch_bounds__(128, 1) peak_tc_kernel(int iters) {
       mma_commit(smem_u32(bar));
       bool done = false;
       for (uint32_t w = 0; w < kTcWaitLimit && !done; ++w) done = mbar_try(smem_u32(bar), phase);
-      if (!done) {
+      if (!done) {  // wait (bounded) once more for the MMAs in flight: TMEM is freed below
         atomicOr(&g_tc_error, 2u);
+        mbar_drain(smem_u32(bar), phase);
         break;
       }
       phase ^= 1;
