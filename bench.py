@@ -363,6 +363,38 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2, mix=None, desc=None):
             "mix": desc or "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
 
 
+def launch_floor(lib, ctx, stream, reps):
+    """The same GEMM launched back to back on one stream (operands stay in L2; the GPU-side launch gap
+    and the kernel alone), and replayed from a CUDA graph holding one gbs_gemm: (ms, ms) per GEMM."""
+    import torch
+    from gemmbitserial_gb300 import _capi
+    sh = C.c_void_p(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            _capi.check(lib.gbs_gemm(ctx._h, sh))
+        e0.record(stream)
+        for _ in range(reps):
+            _capi.check(lib.gbs_gemm(ctx._h, sh))
+        e1.record(stream)
+    stream.synchronize()
+    b2b = e0.elapsed_time(e1) / reps
+    g = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    cap.wait_stream(stream)
+    with torch.cuda.graph(g, stream=cap):
+        _capi.check(lib.gbs_gemm(ctx._h, C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            g.replay()
+        e0.record(stream)
+        for _ in range(reps):
+            g.replay()
+        e1.record(stream)
+    stream.synchronize()
+    return b2b, e0.elapsed_time(e1) / reps
+
+
 def measure_configs(lib, dev, stream, reps=50, warmup=5):
     """Every named workload (C1, C2, C3a, C3b, the adjoint layer's forward): forward time with packed
     operands resident and L2 flushed before each launch, the pipe the built-in rule chose, its rate,
@@ -393,6 +425,7 @@ def measure_configs(lib, dev, stream, reps=50, warmup=5):
                 e1.record(stream)
         stream.synchronize()
         ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+        b2b_ms, graph_ms = launch_floor(lib, ctx, stream, reps)
         res = ctx.res.reshape(N, M)
         ok = hashlib.sha256(np.ascontiguousarray(res).tobytes()).hexdigest() == gold.get(name, {}).get("sha256")
         pipe = ctx.pipe
@@ -422,6 +455,7 @@ def measure_configs(lib, dev, stream, reps=50, warmup=5):
         out[name] = {"ms": round(ms, 4), "gops": round(gops(M, K, N, ms * 1e-3), 1), "pipe": names.get(pipe, pipe),
                      "tbinops": round(2.0 * M * N * kpad * wA * wB / (ms * 1e-3) / 1e12, 2),
                      "gbs_packed_bytes": round(packed / (ms * 1e-3) / 1e9, 1),
+                     "b2b_ms": round(b2b_ms, 4), "graph_replay_ms": round(graph_ms, 4),
                      "tuned": tuned, "pair_kernel": pair_kernel_name(lp),
                      **({"cuda_core_ms": round(cuda_core_ms, 4), "speedup_vs_cuda_cores": round(cuda_core_ms / ms, 1),
                          "how": "operands split into plane parts of <= 4 bits, one digit GEMM per part pair"}
