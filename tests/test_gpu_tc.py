@@ -116,14 +116,19 @@ def test_tc_sums_near_the_exactness_bound():
 
 
 def test_tc_pipe_declines_what_it_cannot_do_exactly():
-    """8-bit operands or K beyond the fp32 bound fall back to the CUDA-core pipe; the
-    shared-memory variants also decline more than 5 planes; AUTO keeps tiny problems
-    on the CUDA cores."""
-    for (M, K, N, wa, wb) in [(128, 256, 128, 8, 1), (128, 1 << 21, 128, 4, 1)]:
-        ctx = allocGEMMContext(M, K, N, wa, wb, False, False)
-        ctx.set_pipe(_capi.GBS_PIPE_TC)
-        assert ctx.pipe == _capi.GBS_PIPE_POPC
-        deallocGEMMContext(ctx)
+    """K beyond the fp32 bound falls back to the CUDA-core pipe (8-bit operands run in plane parts
+    on the digit pipe, but not on the shared-memory variants); the shared-memory variants also
+    decline more than 5 planes; AUTO keeps tiny problems on the CUDA cores."""
+    ctx = allocGEMMContext(128, 1 << 21, 128, 4, 1, False, False)
+    ctx.set_pipe(_capi.GBS_PIPE_TC)
+    assert ctx.pipe == _capi.GBS_PIPE_POPC
+    deallocGEMMContext(ctx)
+    ctx = allocGEMMContext(128, 256, 128, 8, 1, False, False)
+    ctx.set_pipe(_capi.GBS_PIPE_TC)
+    assert ctx.pipe == _capi.GBS_PIPE_TC
+    ctx.set_pipe(_capi.GBS_PIPE_TC_SMEM)
+    assert ctx.pipe == _capi.GBS_PIPE_POPC
+    deallocGEMMContext(ctx)
     ctx = allocGEMMContext(128, 256, 128, 4, 4, False, False)
     ctx.set_pipe(_capi.GBS_PIPE_TC_SMEM)
     assert ctx.pipe == _capi.GBS_PIPE_POPC
