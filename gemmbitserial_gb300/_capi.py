@@ -40,6 +40,8 @@ SIGNATURES = {
     "gbs_import_quantize": (i32, [vp, i32, vp, vp, i32, i32, i32, vp]),
     "gbs_get_bit": (i32, [vp, i32, u64, u64, u64, C.POINTER(i32)]),
     "gbs_set_bit": (i32, [vp, i32, u64, u64, u64, i32]),
+    "gbs_get_word": (i32, [vp, i32, u64, u64, u64, C.POINTER(u64)]),
+    "gbs_set_word": (i32, [vp, i32, u64, u64, u64, u64]),
     "gbs_clear": (i32, [vp, i32, vp]),
     "gbs_gemm": (i32, [vp, vp]),
     "gbs_gemm_to": (i32, [vp, vp, vp]),

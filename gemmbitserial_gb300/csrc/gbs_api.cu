@@ -660,6 +660,37 @@ int gbs_set_bit(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, 
   return GBS_OK;
 }
 
+int gbs_get_word(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, uint64_t *value) {
+  uint64_t *w = nullptr;
+  int rc = bit_word(c, side, bit, row, col, &w, "gbs_get_word");
+  if (rc != GBS_OK) return rc;
+  if (!value) return fail(GBS_EINVAL, "gbs_get_word: value is NULL");
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(value, w, sizeof(uint64_t), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? GBS_OK : cuda_fail(e, "gbs_get_word");
+}
+
+int gbs_set_word(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, uint64_t value) {
+  uint64_t *w = nullptr;
+  int rc = bit_word(c, side, bit, row, col, &w, "gbs_set_word");
+  if (rc != GBS_OK) return rc;
+  Mat &m = side ? c->rhs : c->lhs;
+  // padding stays zero (results never depend on it): rows past nrows take no
+  // bits, and a word's columns past ncols are cleared
+  const uint64_t c0 = col & ~(uint64_t)63;
+  if (row >= m.nrows || c0 >= m.ncols) value = 0;
+  else if (m.ncols - c0 < 64) value &= ((uint64_t)1 << (m.ncols - c0)) - 1;
+  DeviceGuard g(c->device);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(w, &value, sizeof(uint64_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "gbs_set_word");
+  m.imported = true;
+  c->digits_valid[side] = false;  // derived operands no longer match the planes
+  c->vt_valid[side] = false;
+  return GBS_OK;
+}
+
 int gbs_clear(gbs_ctx *c, int side, void *stream) {
   if (!c) return fail(GBS_EINVAL, "gbs_clear: ctx is NULL");
   if (side != GBS_LHS && side != GBS_RHS) return fail(GBS_EINVAL, "gbs_clear: bad side");

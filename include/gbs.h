@@ -196,6 +196,13 @@ GBS_API int gbs_get_planes(gbs_ctx *ctx, int side, uint64_t *dst, void *stream);
 GBS_API int gbs_get_bit(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uint64_t col, int *value);
 GBS_API int gbs_set_bit(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uint64_t col, int value);
 
+/* BitSerialMatrix::word (gemmbitserial.hpp:110-115): the 64-bit plane word
+ * holding (bit, row, col), read or written (the device is synchronised first;
+ * one word moves).  A written word keeps the padding zero: bits of columns
+ * past ncols, and whole words of rows past nrows, are stored as 0. */
+GBS_API int gbs_get_word(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uint64_t col, uint64_t *value);
+GBS_API int gbs_set_word(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uint64_t col, uint64_t value);
+
 /* BitSerialMatrix::clearAll (gemmbitserial.hpp:95-98): zeroes every plane of
  * one side on `stream` (and marks the side imported). */
 GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);

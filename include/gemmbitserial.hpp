@@ -117,6 +117,33 @@ class BitSerialMatrix {
   void set(uint64_t bit, uint64_t row, uint64_t col) { detail::check(gbs_set_bit(ctx_, side_, bit, row, col, 1)); }
   void unset(uint64_t bit, uint64_t row, uint64_t col) { detail::check(gbs_set_bit(ctx_, side_, bit, row, col, 0)); }
   void clearAll() { detail::check(gbs_clear(ctx_, side_, nullptr)); }
+  // word (reference :110-115) returns a uint64_t& into host planes; the planes
+  // live on the device, so here it returns a proxy that reads or writes the
+  // word through the library (padding bits stay zero)
+  class WordRef {
+   public:
+    WordRef(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col)
+        : c_(c), side_(side), bit_(bit), row_(row), col_(col) {}
+    operator uint64_t() const {
+      uint64_t v = 0;
+      detail::check(gbs_get_word(c_, side_, bit_, row_, col_, &v));
+      return v;
+    }
+    WordRef &operator=(uint64_t v) {
+      detail::check(gbs_set_word(c_, side_, bit_, row_, col_, v));
+      return *this;
+    }
+    WordRef &operator=(const WordRef &o) { return *this = (uint64_t)o; }
+    WordRef &operator|=(uint64_t v) { return *this = (uint64_t)*this | v; }
+    WordRef &operator&=(uint64_t v) { return *this = (uint64_t)*this & v; }
+    WordRef &operator^=(uint64_t v) { return *this = (uint64_t)*this ^ v; }
+
+   private:
+    gbs_ctx *c_;
+    int side_;
+    uint64_t bit_, row_, col_;
+  };
+  WordRef word(uint64_t bit, uint64_t row, uint64_t col) { return WordRef(ctx_, side_, bit, row, col); }
   // DEVICE pointers into the planes (reference :117-124)
   uint64_t *rowptr(uint64_t bit, uint64_t row) { return data + bit * wordsPerBitplane() + row * wordsPerRow(); }
   uint64_t *bitplaneptr(uint64_t bit) { return data + bit * wordsPerBitplane(); }

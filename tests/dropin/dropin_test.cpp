@@ -81,6 +81,25 @@ int main() {
     deallocGEMMContext(g);
     failed += report("padding", ok, total);
   }
+  {  // word(): read, write and or-assign through the device proxy; padding bits stay zero
+    int ok = 0, total = 0;
+    BitSerialMatrix m = BitSerialMatrix::alloc(2, 5, 100, false, 8);  // rows 5..7 are padding
+    m.word(1, 3, 70) = 0xF0F0F0F0F0F0F0F0ull;  // columns 64..99 of row 3: bits past column 99 are dropped
+    ok += (uint64_t)m.word(1, 3, 70) == (0xF0F0F0F0F0F0F0F0ull & ((1ull << 36) - 1));
+    total++;
+    m.word(0, 2, 5) |= 0x21ull;
+    ok += m.get(0, 2, 0) && m.get(0, 2, 5) && !m.get(0, 2, 1);
+    total++;
+    m.unset(0, 2, 0);
+    ok += (uint64_t)m.word(0, 2, 0) == 0x20ull;
+    total++;
+    m.word(0, 4, 0) = ~0ull;
+    m.word(0, 5, 0) = ~0ull;  // a padding row: stays zero
+    ok += (uint64_t)m.word(0, 4, 0) == ~0ull && (uint64_t)m.word(0, 5, 0) == 0;  // columns 0..63 all exist
+    total++;
+    BitSerialMatrix::dealloc(m);
+    failed += report("word", ok, total);
+  }
   {  // sumRows on a copy of ctx.lhs, all d sums
     int ok = 0, total = 0;
     for (int b : {1, 2, 3, 4})

@@ -129,3 +129,30 @@ def test_gemm_sees_bit_edits(pipe):
         assert not np.any(ctx.res)
     finally:
         deallocGEMMContext(ctx)
+
+
+def test_word_get_set_through_the_abi(gbs_lib):
+    """gbs_get_word / gbs_set_word (BitSerialMatrix::word): one device word; padding stays zero, and a
+    GEMM after a word write sees the new bits."""
+    import ctypes as C
+    lib = gbs_lib
+    M, K, N = 40, 100, 30
+    A = datagen.operand(datagen.SEED_BASE + 990, M, K, 2, "u")
+    B = datagen.operand(datagen.SEED_BASE + 991, N, K, 1, "u")
+    ctx = allocGEMMContext(M, K, N, 2, 1, False, False)
+    try:
+        ctx.lhs.importRegular(A)
+        ctx.rhs.importRegular(B)
+        v = C.c_uint64()
+        _capi.check(lib.gbs_get_word(ctx._h, 0, 1, 7, 70, C.byref(v)))
+        want = sum(((int(A[7, c]) >> 1) & 1) << (c - 64) for c in range(64, K))
+        assert v.value == want
+        _capi.check(lib.gbs_set_word(ctx._h, 0, 1, 7, 70, 0xFFFFFFFFFFFFFFFF))
+        _capi.check(lib.gbs_get_word(ctx._h, 0, 1, 7, 70, C.byref(v)))
+        assert v.value == (1 << (K - 64)) - 1  # columns past K stay zero
+        A2 = A.copy()
+        A2[7, 64:] |= 2
+        gemmBitSerial(ctx)
+        assert np.array_equal(ctx.res.reshape(N, M), O.oracle_gemm(A2, B, 2, 1, False, False))
+    finally:
+        deallocGEMMContext(ctx)
