@@ -19,6 +19,7 @@ prints "ok <case>".  The kernels each case launches:
   expand          column-major imports, then a forward that first expands the planes (expand_one_kernel)
   group           the 512-problem mix as one group: import, row sums, GEMMs (pack_grouped, rowsum_grouped,
                   gemm_tcg_kernel, gemm_popc_grouped)
+  group_small     the same on a 96-problem mix of the same distribution (a few hundred MB on the device)
   adjoint         A 4096x2048 u2, B 2048x2048 bipolar, dC ~ N(0,1) (split_kernel, values_t_kernel, adjoint_tc_kernel)
   adjoint_simt    the same on the CUDA cores (adjoint_kernel)
 """
@@ -30,7 +31,8 @@ import os
 import sys
 
 CASES = ["gemm", "gemm_streamk", "gemm_popc", "gemm_bmma", "gemm_tc_smem", "gemm_skinny", "import_device",
-         "import_host", "import_colmajor", "import_quantize", "expand", "group", "adjoint", "adjoint_simt"]
+         "import_host", "import_colmajor", "import_quantize", "expand", "group", "group_small", "adjoint",
+         "adjoint_simt"]
 
 
 def main() -> None:
@@ -104,9 +106,9 @@ def main() -> None:
             _capi.check(lib.gbs_import(c._h, 0, C.c_void_p(aT.data_ptr()), _capi.GBS_I8, 1, sh))
             _capi.check(lib.gbs_import(c._h, 1, C.c_void_p(bT.data_ptr()), _capi.GBS_I8, 1, sh))
             _capi.check(lib.gbs_gemm(c._h, sh))
-    elif case == "group":
+    elif case in ("group", "group_small"):
         from gemmbitserial_gb300.grouped import Group
-        mix = datagen.grouped_mix()
+        mix = datagen.grouped_mix() if case == "group" else datagen.grouped_mix(seed=datagen.SEED_BASE + 77, count=96)
         gen = torch.Generator(device=dev)
         gen.manual_seed(4321)
         ops = [(datagen.torch_operand(gen, M, K, wA, eA, dev), datagen.torch_operand(gen, N, K, wB, eB, dev))
