@@ -250,99 +250,70 @@ __device__ __forceinline__ int find_job(const PackJob *jobs, int njobs, uint64_t
 // Grouped import: one launch packs every operand of a grouped GEMM
 // (row-major sources); units (1024-column segments of a row) are numbered
 // across the jobs.  A warp takes kRun consecutive units: one job lookup,
-// then the units in order.  For 1-byte sources (the vector path) each lane
-// stages its 32 input bytes of the next kStageDepth units in its own slots
-// of shared memory with cp.async (zero-filled past the row or the matrix), so
-// the bytes in flight do not occupy registers: the previous form, one unit
-// prefetched into registers, held 64 registers per thread, 4 blocks per SM and
-// ~42 % of HBM; staged, it fits 48 registers and 5 blocks of 32 KB per SM.
-// Other element types load directly when a unit is packed.
+// then the units in order.
 constexpr int kRun = 8;
-constexpr int kStageDepth = 4;
 
-__device__ __forceinline__ void cp_async16_zfill(uint32_t dst, const void *src, bool pred) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(pred ? 16 : 0)
-               : "memory");
-}
-
-__global__ void __launch_bounds__(256, 5) pack_grouped(const PackJob *__restrict__ jobs, int njobs, uint64_t total) {
-  __shared__ __align__(16) uint4 stage[kStageDepth][256][2];  // [slot][thread][two 16-byte halves]
+__global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ jobs, int njobs, uint64_t total) {
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const int t = threadIdx.x, lane = t & 31;
-  // unit w -> (job, row, segment), advancing the job index monotonically
-  auto locate = [&](uint64_t w, int &jj, uint64_t &r, uint64_t &sg) {
-    while (jj + 1 < njobs && jobs[jj + 1].warp0 <= w) jj++;
-    const PackJob &J = jobs[jj];
-    const uint64_t local = w - J.warp0;
-    if (local < 0xFFFFFFFFull) {  // 32-bit division in the common case
-      const uint32_t l32 = (uint32_t)local, r32 = l32 / J.segs;
-      r = r32;
-      sg = l32 - r32 * J.segs;
-    } else {
-      r = local / J.segs;
-      sg = local % J.segs;
-    }
-  };
-  // stages unit w's 32 bytes for this lane (vector-path jobs only); always commits one group
-  auto issue = [&](uint64_t w, int &jj, int slot) {
-    uint64_t r, sg;
-    locate(w, jj, r, sg);
-    const PackJob &J = jobs[jj];
-    const uint64_t col0 = sg * kSegCols + (uint64_t)lane * 32;
-    if (J.vec && col0 < J.wpr * 64) {
-      const bool in = r < J.nrows && col0 < J.ncols;
-      const uint8_t *p = (const uint8_t *)J.src + (in ? r * J.ncols + col0 : 0);
-      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&stage[slot][t][0]);
-      cp_async16_zfill(dst, p, in);
-      cp_async16_zfill(dst + 16, in ? p + 16 : p, in && col0 + 32 <= J.ncols);
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-  };
+  const int lane = threadIdx.x & 31;
   for (uint64_t base = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRun; base < total;
        base += nw * kRun) {
-    const int j0 = find_job(jobs, njobs, base);
-    const int n = (int)min((uint64_t)kRun, total - base);
-    int ji = j0, jp = j0;  // job cursors of the issue and the pack sides
-#pragma unroll
-    for (int i = 0; i < kStageDepth; i++) {
-      if (i < n) issue(base + i, ji, i);
-      else asm volatile("cp.async.commit_group;\n" ::: "memory");
-    }
-#pragma unroll
-    for (int i = 0; i < kRun; i++) {
-      if (i >= n) break;
-      asm volatile("cp.async.wait_group %0;\n" ::"n"(kStageDepth - 1) : "memory");
-      uint64_t rc, sc;
-      locate(base + i, jp, rc, sc);
-      const PackJob &J = jobs[jp];
+    int j = find_job(jobs, njobs, base);
+    // unit w -> (job, row, segment), advancing the job index monotonically
+    auto locate = [&](uint64_t w, int &jj, uint64_t &r, uint64_t &sg) {
+      while (jj + 1 < njobs && jobs[jj + 1].warp0 <= w) jj++;
+      const PackJob &J = jobs[jj];
+      const uint64_t local = w - J.warp0;
+      if (local < 0xFFFFFFFFull) {  // 32-bit division in the common case
+        const uint32_t l32 = (uint32_t)local, r32 = l32 / J.segs;
+        r = r32;
+        sg = l32 - r32 * J.segs;
+      } else {
+        r = local / J.segs;
+        sg = local % J.segs;
+      }
+    };
+    auto load = [&](int jj, uint64_t r, uint64_t sg, uint32_t (&q)[8]) {
+      const PackJob &J = jobs[jj];
+      const uint64_t col0 = sg * kSegCols + (uint64_t)lane * 32;
+      if (col0 < J.wpr * 64)
+        load_codes32(J.src, J.dtype, J.nbits == 1 && J.issigned, J.issigned, J.nbits, J.nrows, J.ncols, J.vec, r,
+                     col0, q);
+    };
+    // the next unit's loads are in flight while the current unit is packed
+    const uint64_t last = min(base + (uint64_t)kRun, total);
+    int jc = j;
+    uint64_t rc, sc;
+    locate(base, jc, rc, sc);
+    uint32_t q[8];
+    load(jc, rc, sc, q);
+#pragma unroll 1
+    for (uint64_t w = base; w < last; w++) {
+      int jn = jc;
+      uint64_t rn = 0, sn = 0;
+      uint32_t qn[8];
+      if (w + 1 < last) {
+        locate(w + 1, jn, rn, sn);
+        load(jn, rn, sn, qn);
+      }
+      const PackJob &J = jobs[jc];
       const uint64_t col0 = sc * kSegCols + (uint64_t)lane * 32;
       if (col0 < J.wpr * 64) {
-        uint32_t q[8];
-        if (J.vec) {  // this lane's own staged bytes (no other lane reads them)
-          const uint4 v0 = stage[i % kStageDepth][t][0], v1 = stage[i % kStageDepth][t][1];
-          q[0] = v0.x; q[1] = v0.y; q[2] = v0.z; q[3] = v0.w;
-          q[4] = v1.x; q[5] = v1.y; q[6] = v1.z; q[7] = v1.w;
-          if (J.nbits == 1 && J.issigned && J.dtype == GBS_I8) {
-#pragma unroll
-            for (int k = 0; k < 8; k++) q[k] = __vcmpgts4(q[k], 0u) & 0x01010101u;
-          }
-        } else {
-          load_codes32(J.src, J.dtype, J.nbits == 1 && J.issigned, J.issigned, J.nbits, J.nrows, J.ncols, 0, rc,
-                       col0, q);
-        }
         emit_planes32(J.nbits, J.nrows_a, J.wpr, J.planes, rc, col0, q);
         if (J.digits && rc < J.nrows) {
           const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
           write_digits32(J.digits, J.nbits, J.nrows, J.ncols, J.dcols, tab, rc, col0, q);
         }
       }
-      // the slot just read takes unit i + kStageDepth (the reads above completed: they are
-      // ordinary loads of this lane, ordered before its next cp.async to the same address)
-      if (i + kStageDepth < n) issue(base + i + kStageDepth, ji, i % kStageDepth);
-      else asm volatile("cp.async.commit_group;\n" ::: "memory");
+      if (w + 1 < last) {
+        jc = jn;
+        rc = rn;
+        sc = sn;
+#pragma unroll
+        for (int i = 0; i < 8; i++) q[i] = qn[i];
+      }
     }
   }
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 // Column-major pack (the reference's readColMajor: element (r, c) at c*nrows + r).
