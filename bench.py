@@ -349,6 +349,10 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2, mix=None, desc=None):
         deallocGEMMContext(c)
     gops_total = sum(2.0 * M * K * N for (M, K, N, *_r) in mix)
     binops = sum(2.0 * M * N * ((K + 63) // 64 * 64) * wA * wB for (M, K, N, wA, _a, wB, _b) in mix)
+    # algorithmic HBM bytes of the GEMMs: both operands' packed planes read once, the int32 results written
+    alg_bytes = sum((M * wA + N * wB) * ((K + 63) // 64) * 8 + 4.0 * M * N for (M, K, N, wA, _a, wB, _b) in mix)
+    hbm = measured_peaks().get("hbm_gbs")
+    achieved_gbs = alg_bytes / (t_group * 1e-3) / 1e9
     return {"problems": len(mix), "plain_gemm_ms": round(t_plain, 4), "grouped_gemm_ms": round(t_group, 4),
             "speedup_gemm": round(t_plain / t_group, 3),
             "plain_pack_gemm_ms": round(t_plain_full, 4), "graph_pack_gemm_ms": round(t_graph, 4),
@@ -358,7 +362,11 @@ def measure_grouped(lib, dev, stream, reps=5, warmup=2, mix=None, desc=None):
             "grouped_tbinops": round(binops / (t_group * 1e-3) / 1e12, 2),
             "tiles": stats["tiles"], "grid": stats["grid"], "smem_bytes": stats["smem_bytes"],
             "popc_problems": stats["popc_problems"], "tc_problems": stats["tc_problems"],
-            "tc_tiles": stats["tc_tiles"],
+            "tc_tiles": stats["tc_tiles"], "tc_kernel": stats["tc_kernel"],
+            "hbm_roofline": {"algorithmic_bytes": alg_bytes, "achieved": round(achieved_gbs, 1), "unit": "GB/s",
+                             "peak": hbm, "frac": round(achieved_gbs / hbm, 4) if hbm else None,
+                             "bytes": "packed planes of both operands + int32 results, per grouped GEMM launch",
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)" if hbm else None},
             "parity": "grouped == plain (sampled 14 problems)" if ok else "MISMATCH",
             "mix": desc or "M log-uniform [1,256], K = 64*U{4..128}, N = U{64..4096}, wA {1,2,4}, wB {1,2,3,4}, u/s/b"}
 

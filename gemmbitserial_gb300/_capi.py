@@ -66,6 +66,7 @@ SIGNATURES = {
     "gbs_group_split": (i32, [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
     "gbs_group_free": (i32, [vp]),
     "gbs_debug_group_poison_tile": (i32, [vp, C.c_uint32]),
+    "gbs_debug_group_tc_kernel": (i32, [vp]),
     "gbs_pipe_peaks": (i32, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gbs_tune": (i32, [vp, i32, C.POINTER(i32), vp]),
     "gbs_tuner_save": (i32, [C.c_char_p]),

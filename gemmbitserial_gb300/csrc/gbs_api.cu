@@ -132,6 +132,8 @@ void free_ctx_buffers(gbs_ctx *c) {
   if (c->sk_flags) cudaFree(c->sk_flags);
   if (c->digits[0]) cudaFree(c->digits[0]);
   if (c->digits[1]) cudaFree(c->digits[1]);
+  if (c->nibbles[0]) cudaFree(c->nibbles[0]);
+  if (c->nibbles[1]) cudaFree(c->nibbles[1]);
 }
 
 // The reference's padding of a context's bit planes, restated:
@@ -447,7 +449,7 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
   DeviceGuard g(c->device);
   if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_import: cudaSetDevice");
   cudaStream_t s = as_stream(stream);
-  c->digits_valid[side] = false;
+  c->digits_valid[side] = c->nibbles_valid[side] = false;
   c->vt_valid[side] = false;
   uint8_t *digits = nullptr;
   uint32_t dtab[4] = {0, 0, 0, 0};
@@ -548,7 +550,7 @@ int gbs_import_quantize(gbs_ctx *c, int side, const void *src, const void *thres
   DeviceGuard g(c->device);
   if (!g.ok) return cuda_fail(cudaGetLastError(), "gbs_import_quantize: cudaSetDevice");
   cudaStream_t s = as_stream(stream);
-  c->digits_valid[side] = false;
+  c->digits_valid[side] = c->nibbles_valid[side] = false;
   c->vt_valid[side] = false;
   uint8_t *digits = nullptr;
   uint32_t dtab[4] = {0, 0, 0, 0};
@@ -655,7 +657,7 @@ int gbs_set_bit(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col, 
   if (e != cudaSuccess) return cuda_fail(e, "gbs_set_bit");
   Mat &m = side ? c->rhs : c->lhs;
   m.imported = true;
-  c->digits_valid[side] = false;  // derived operands no longer match the planes
+  c->digits_valid[side] = c->nibbles_valid[side] = false;  // derived operands no longer match the planes
   c->vt_valid[side] = false;
   return GBS_OK;
 }
@@ -686,7 +688,7 @@ int gbs_set_word(gbs_ctx *c, int side, uint64_t bit, uint64_t row, uint64_t col,
   if (e == cudaSuccess) e = cudaMemcpy(w, &value, sizeof(uint64_t), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_set_word");
   m.imported = true;
-  c->digits_valid[side] = false;  // derived operands no longer match the planes
+  c->digits_valid[side] = c->nibbles_valid[side] = false;  // derived operands no longer match the planes
   c->vt_valid[side] = false;
   return GBS_OK;
 }
@@ -701,7 +703,7 @@ int gbs_clear(gbs_ctx *c, int side, void *stream) {
     if (e != cudaSuccess) return cuda_fail(e, "gbs_clear");
   }
   m.imported = true;
-  c->digits_valid[side] = false;
+  c->digits_valid[side] = c->nibbles_valid[side] = false;
   c->vt_valid[side] = false;
   return GBS_OK;
 }

@@ -1319,6 +1319,21 @@ bool tc_map_u8(void *map, const uint8_t *base, uint64_t cols, uint64_t rows, uin
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Map of a nibble matrix (rows x cols codes, blocks of nibble_offset) as the
+// 4-D tensor [rows/16][cols/128][16][64] bytes; a box is 256 rows of one
+// 128-column chunk, 64-byte swizzled.
+bool tc_map_nibbles(void *map, const uint8_t *base, uint64_t cols, uint64_t rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || cols % 128 || rows % 256 || rows == 0) return false;
+  cuuint64_t dims[4] = {64, 16, cols / 128, rows / 16};
+  cuuint64_t strides[3] = {64, 1024, (cols / 128) * 1024};
+  cuuint32_t box[4] = {64, 16, 1, 16};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  return fn(reinterpret_cast<CUtensorMap *>(map), CU_TENSOR_MAP_DATA_TYPE_UINT8, 4, (void *)base, dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 void tc_digit_table(const Mat &m, uint32_t tab[4]) {
   const TcOperand op = make_operand(m, true);
   for (int i = 0; i < 4; i++) tab[i] = op.tab[0][i];
@@ -1404,6 +1419,14 @@ cudaError_t expand_side(gbs_ctx *c, int side, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   e = launch_expand(make_expand_job(side ? c->rhs : c->lhs, c->digits[side]), s);
   if (e == cudaSuccess) c->digits_valid[side] = true;
+  return e;
+}
+
+cudaError_t expand_nibble_side(gbs_ctx *c, int side, cudaStream_t s) {
+  cudaError_t e = ensure_nibble_buffer(c, side);
+  if (e != cudaSuccess) return e;
+  e = launch_expand(make_nibble_job(side ? c->rhs : c->lhs, c->nibbles[side]), s);
+  if (e == cudaSuccess) c->nibbles_valid[side] = true;
   return e;
 }
 
@@ -1640,6 +1663,26 @@ bool pdl_enabled() {
 }
 
 cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
+  if (bn_req < 0 && (c->lhs.nrows < 256 || c->rhs.nrows < 256)) {
+    // a side of fewer than 256 rows: the persistent kernel over a one-problem
+    // plan (larger side as the MMA's 128-row operand, MMA N down to 16)
+    if (!c->plan1_ready) {
+      if (!c->plan1) c->plan1 = new TcgPlan();
+      gbs_ctx *one[1] = {c};
+      if (tcg_plan_build(c->plan1, one, 1) != GBS_OK) return cudaErrorInvalidValue;
+      c->plan1_ready = true;
+    }
+    for (int side = 0; side < 2; side++) {  // the digit and nibble matrices the plan reads
+      cudaError_t e = cudaSuccess;
+      if (((c->plan1->sides[0] >> side) & 1) && !c->digits_valid[side]) e = expand_side(c, side, s);
+      if (e == cudaSuccess && ((c->plan1->sides[0] >> (2 + side)) & 1) && !c->nibbles_valid[side])
+        e = expand_nibble_side(c, side, s);
+      if (e != cudaSuccess) return e;
+    }
+    uint32_t *err = tc_error_ptr();
+    if (!err) return cudaErrorInvalidSymbol;
+    return tcg_gemm(*c->plan1, err, s, c->out);
+  }
   for (int side = 0; side < 2; side++)
     if (!c->digits_valid[side]) {
       cudaError_t e = expand_side(c, side, s);
@@ -1657,19 +1700,6 @@ cudaError_t launch_gemm_tc_hbm(gbs_ctx *c, cudaStream_t s, int bn_req) {
   a.M = c->lhs.nrows;
   a.N = c->rhs.nrows;
   a.nstages = (uint32_t)(c->lhs.dcols / 128);
-  if (bn_req < 0 && (a.M < 256 || a.N < 256)) {
-    // a side of fewer than 256 rows: the persistent kernel over a one-problem
-    // plan (larger side as the MMA's 128-row operand, MMA N down to 16)
-    if (!c->plan1_ready) {
-      if (!c->plan1) c->plan1 = new TcgPlan();
-      gbs_ctx *one[1] = {c};
-      if (tcg_plan_build(c->plan1, one, 1) != GBS_OK) return cudaErrorInvalidValue;
-      c->plan1_ready = true;
-    }
-    uint32_t *err = tc_error_ptr();
-    if (!err) return cudaErrorInvalidSymbol;
-    return tcg_gemm(*c->plan1, err, s, c->out);
-  }
   if (bn_req == kPairVariantStreamK) return launch_pair_streamk(c, s, a);
   if (bn_req == kPairVariant || bn_req == kPairVariant128 || bn_req == kPairVariantPersistent || bn_req < 0 ||
       pair_split_variant(bn_req)) {

@@ -28,6 +28,7 @@
 // Every mbarrier wait is bounded; on timeout the CTA sets a bit in the
 // caller's error word, stops issuing, drains what it issued and frees TMEM.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -255,6 +256,32 @@ __device__ __forceinline__ void expand_chunk(const ExpandJob &j, uint32_t r, uin
   *reinterpret_cast<uint4 *>(j.digits + digit_offset(r, col0, j.dcols)) = make_uint4(q[0], q[1], q[2], q[3]);
 }
 
+// One thread writes 32 codes (one 16-byte store) of one row of a nibble
+// matrix: the codes of 4 columns as bytes (plane p's nibble spread to bit p
+// of each byte), then two bytes' codes into one (even column low).
+template <int CNT>
+__device__ __forceinline__ void expand_nibble_chunk(const ExpandJob &j, uint32_t r, uint32_t col0) {
+  const uint64_t w = col0 >> 6;
+  const int sh = (int)(col0 & 63);
+  uint32_t pw[CNT];
+#pragma unroll
+  for (int p = 0; p < CNT; p++) pw[p] = (uint32_t)(j.planes[(p * j.nrows_a + r) * j.wpr + w] >> sh);
+  uint32_t o[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {  // columns 8i .. 8i + 7
+    uint32_t t[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      uint32_t c = 0;
+#pragma unroll
+      for (int p = 0; p < CNT; p++) c |= (bfe4(pw[p], 8 * i + 4 * h) * (0x00204081u << p)) & (0x01010101u << p);
+      t[h] = c | (c >> 4);  // bytes 0 and 2: code pairs (even column low)
+    }
+    o[i] = __byte_perm(t[0], t[1], 0x6420u);
+  }
+  *reinterpret_cast<uint4 *>(j.digits + nibble_offset(r, col0, j.dcols)) = make_uint4(o[0], o[1], o[2], o[3]);
+}
+
 __device__ __forceinline__ void expand_thread(const ExpandJob &j, uint64_t local) {
   if (local >= (uint64_t)j.nrows * j.chunks) return;  // padding threads of the job
   uint32_t r, col0;
@@ -264,6 +291,16 @@ __device__ __forceinline__ void expand_thread(const ExpandJob &j, uint64_t local
   } else {
     r = (uint32_t)(local / j.chunks);
     col0 = (uint32_t)(local % j.chunks) * 16u;
+  }
+  if (j.nib) {
+    col0 *= 2;  // 32 codes per thread
+    switch (j.nbits) {
+      case 1: expand_nibble_chunk<1>(j, r, col0); break;
+      case 2: expand_nibble_chunk<2>(j, r, col0); break;
+      case 3: expand_nibble_chunk<3>(j, r, col0); break;
+      default: expand_nibble_chunk<4>(j, r, col0); break;
+    }
+    return;
   }
   switch (j.nbits) {
     case 1: expand_chunk<1>(j, r, col0); break;
@@ -327,6 +364,13 @@ ExpandJob make_expand_job(const Mat &m, uint8_t *digits) {
   return j;
 }
 
+ExpandJob make_nibble_job(const Mat &m, uint8_t *nibbles) {
+  ExpandJob j = make_expand_job(m, nibbles);
+  j.nib = 1;
+  j.chunks = (uint32_t)((m.ncols + 31) / 32);
+  return j;
+}
+
 cudaError_t launch_expand(const ExpandJob &job, cudaStream_t s) {
   const uint64_t threads = (uint64_t)job.nrows * job.chunks;
   if (threads == 0) return cudaSuccess;
@@ -351,6 +395,19 @@ cudaError_t ensure_digit_buffer(gbs_ctx *c, int side) {
   return e;
 }
 
+// Nibble matrix [drows][dcols / 2] of one side, allocated zeroed on first use.
+cudaError_t ensure_nibble_buffer(gbs_ctx *c, int side) {
+  if (c->nibbles[side]) return cudaSuccess;
+  const Mat &m = side ? c->rhs : c->lhs;
+  const size_t bytes = std::max<size_t>(m.drows * m.dcols / 2, 16);
+  cudaError_t e = dev_alloc((void **)&c->nibbles[side], bytes);
+  if (e == cudaSuccess) e = cudaMemset(c->nibbles[side], 0, bytes);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  c->plan1_ready = false;
+  c->nibbles_valid[side] = false;
+  return e;
+}
+
 // The digit kernel is exact when every partial sum stays below 2^24 in fp32
 // and each operand's values fit e4m3 exactly (at most 4 bits).
 bool tcg_eligible(const gbs_ctx *c) { return tc_exact(c, GBS_PIPE_TC); }
@@ -371,8 +428,21 @@ void tcg_plan_free(TcgPlan *p) {
   *p = TcgPlan();
 }
 
+namespace {
+
+// GBS_TCG_NIBBLES=0 in the environment keeps the plans built from then on on
+// the digit kernel.
+bool nibbles_enabled() {
+  const char *v = getenv("GBS_TCG_NIBBLES");
+  return !(v && v[0] == '0');
+}
+
+}  // namespace
+
 int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
   tcg_plan_free(plan);
+  const bool nib = nibbles_enabled();
+  plan->nibbles = nib;
   std::vector<TcgProblem> probs;
   std::vector<CUtensorMap> maps;
   std::vector<TcgTile> tiles;
@@ -381,32 +451,54 @@ int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
   uint64_t threads = 0;
   for (int i = 0; i < n; i++) {
     gbs_ctx *c = ctxs[i];
-    for (int side = 0; side < 2; side++)
-      if (ensure_digit_buffer(c, side) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(GBS_ENOMEM, "tensor-core plan: digit matrix allocation failed");
-      }
-    plan->ctxs.push_back(c);
     const Mat &L = c->lhs, &R = c->rhs;
     TcgProblem P;
     memset(&P, 0, sizeof(P));
     P.C = c->res;
     P.M = (uint32_t)L.nrows;
     P.N = (uint32_t)R.nrows;
-    P.swap = L.nrows < R.nrows ? 1u : 0u;
-    const Mat &MA = P.swap ? R : L, &MB = P.swap ? L : R;
-    const uint8_t *da = c->digits[P.swap ? 1 : 0], *db = c->digits[P.swap ? 0 : 1];
+    // digit kernel: the larger side is MMA-A; nibble kernel: the smaller side
+    P.swap = nib ? (R.nrows < L.nrows ? 1u : 0u) : (L.nrows < R.nrows ? 1u : 0u);
+    const int sa = P.swap ? 1 : 0, sb = 1 - sa;  // sides of MMA-A and MMA-B
+    const uint8_t sides = nib ? (uint8_t)((1u << sa) | (4u << sb)) : (uint8_t)3;
+    for (int side = 0; side < 2; side++) {
+      cudaError_t e = cudaSuccess;
+      if ((sides >> side) & 1) e = ensure_digit_buffer(c, side);
+      if (e == cudaSuccess && ((sides >> (2 + side)) & 1)) e = ensure_nibble_buffer(c, side);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GBS_ENOMEM, "tensor-core plan: digit or nibble matrix allocation failed");
+      }
+    }
+    plan->ctxs.push_back(c);
+    plan->sides.push_back(sides);
+    const Mat &MA = sa ? R : L, &MB = sb ? R : L;
     P.a_rows = (uint32_t)MA.drows;
     P.b_rows = (uint32_t)MB.drows;
     P.nk = (uint32_t)((L.ncols + 127) / 128);
-    P.bn = (uint32_t)std::min<uint64_t>(256, (MB.nrows + 15) / 16 * 16);
-    P.idesc = (1u << 4) | ((P.bn >> 3) << 17) | ((128u >> 4) << 24);
     CUtensorMap m2[2];
-    if (!tc_map_u8(&m2[0], da, MA.dcols, MA.drows, 128) || !tc_map_u8(&m2[1], db, MB.dcols, MB.drows, P.bn))
-      return fail(GBS_EUNSUPPORTED, "tensor-core plan: tensor map encoding failed");
+    uint32_t rt, ct;
+    if (!nib) {
+      P.bn = (uint32_t)std::min<uint64_t>(256, (MB.nrows + 15) / 16 * 16);
+      P.idesc = (1u << 4) | ((P.bn >> 3) << 17) | ((128u >> 4) << 24);
+      if (!tc_map_u8(&m2[0], c->digits[sa], MA.dcols, MA.drows, 128) ||
+          !tc_map_u8(&m2[1], c->digits[sb], MB.dcols, MB.drows, P.bn))
+        return fail(GBS_EUNSUPPORTED, "tensor-core plan: tensor map encoding failed");
+      rt = (uint32_t)((MA.nrows + 127) / 128);
+      ct = (uint32_t)((MB.nrows + P.bn - 1) / P.bn);
+    } else {
+      P.bn = 256;
+      P.idesc = (1u << 4) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+      P.w4 = MB.nbits > 3 ? 1u : 0u;
+      tc_digit_table(MB, P.tab);
+      if (!tc_map_u8(&m2[0], c->digits[sa], MA.dcols, MA.drows, 128) ||
+          !tc_map_nibbles(&m2[1], c->nibbles[sb], MB.dcols, MB.drows))
+        return fail(GBS_EUNSUPPORTED, "tensor-core plan: tensor map encoding failed");
+      rt = (uint32_t)((MA.nrows + 127) / 128);
+      ct = (uint32_t)((MB.nrows + 255) / 256);
+    }
     maps.push_back(m2[0]);
     maps.push_back(m2[1]);
-    const uint32_t rt = (uint32_t)((MA.nrows + 127) / 128), ct = (uint32_t)((MB.nrows + P.bn - 1) / P.bn);
     for (uint32_t r = 0; r < rt; r++)
       for (uint32_t cc = 0; cc < ct; cc++) {
         tiles.push_back(TcgTile{(uint32_t)probs.size(), r, cc, 0u});
@@ -415,10 +507,13 @@ int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
     probs.push_back(P);
     for (int side = 0; side < 2; side++) {
       const Mat &m = side ? R : L;
-      ExpandJob j = make_expand_job(m, c->digits[side]);
-      j.thread0 = threads;
-      threads += ((uint64_t)j.nrows * j.chunks + 255) / 256 * 256;
-      if (j.nrows && j.chunks) jobs.push_back(j);
+      for (int kind = 0; kind < 2; kind++) {  // digits, nibbles
+        if (!((sides >> (2 * kind + side)) & 1)) continue;
+        ExpandJob j = kind ? make_nibble_job(m, c->nibbles[side]) : make_expand_job(m, c->digits[side]);
+        j.thread0 = threads;
+        threads += ((uint64_t)j.nrows * j.chunks + 255) / 256 * 256;
+        if (j.nrows && j.chunks) jobs.push_back(j);
+      }
     }
   }
   std::vector<size_t> order(tiles.size());
@@ -432,12 +527,15 @@ int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
   if (e == cudaSuccess) e = upload(&plan->d_tiles, sorted.data(), sorted.size());
   if (e == cudaSuccess) e = upload(&plan->d_jobs, jobs.data(), jobs.size());
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(gemm_tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcg_smem_bytes());
+    e = nib ? tcgn_prepare()
+            : cudaFuncSetAttribute(gemm_tcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tcg_smem_bytes());
   if (e != cudaSuccess) {
     cudaGetLastError();
     tcg_plan_free(plan);
     return fail(GBS_ENOMEM, "tensor-core plan: table upload failed");
   }
+  plan->nibbles = nib;
   plan->nprob = (uint32_t)probs.size();
   plan->ntiles = (uint32_t)sorted.size();
   plan->njobs = (int)jobs.size();
@@ -454,12 +552,17 @@ cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  for (gbs_ctx *c : plan.ctxs) c->digits_valid[0] = c->digits_valid[1] = true;
+  for (size_t i = 0; i < plan.ctxs.size(); i++)
+    for (int side = 0; side < 2; side++) {
+      if ((plan.sides[i] >> side) & 1) plan.ctxs[i]->digits_valid[side] = true;
+      if ((plan.sides[i] >> (2 + side)) & 1) plan.ctxs[i]->nibbles_valid[side] = true;
+    }
   return cudaSuccess;
 }
 
 cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s, int32_t *out0) {
   if (!plan.ntiles) return cudaSuccess;
+  if (plan.nibbles) return tcgn_gemm(plan, err, s, out0);
   gemm_tcg_kernel<<<plan.grid, kTgThreads, tcg_smem_bytes(), s>>>(
       plan.d_probs, reinterpret_cast<const CUtensorMap *>(plan.d_maps), plan.d_tiles, plan.ntiles, plan.nprob, err,
       out0);

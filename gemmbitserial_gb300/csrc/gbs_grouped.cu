@@ -92,7 +92,9 @@ cudaError_t upload(T **dst, const std::vector<T> &v) {
 int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs, const int *dtypes) {
   std::vector<PackJob> jobs;
   uint64_t warps = 0;
+  size_t ti = 0;  // index among the tensor-core problems
   for (size_t p = 0; p < g->ctxs.size(); p++) {
+    const uint8_t digit_sides = g->is_tc[p] ? g->tc.sides[ti++] : 0;
     for (int side = 0; side < 2; side++) {
       const void *src = side ? rhs[p] : lhs[p];
       const int dt = dtypes ? dtypes[2 * p + side] : GBS_I8;
@@ -115,10 +117,11 @@ int build_pack_jobs(gbs_group *g, const void *const *lhs, const void *const *rhs
       j.vec = (dt == GBS_I8 || dt == GBS_U8) && m.ncols % 16 == 0 && ((uintptr_t)src % 16) == 0;
       j.segs = (uint32_t)pack_segs_per_row(m.wpr());
       j.dcols = m.dcols;
-      if (g->is_tc[p]) {  // tensor-core problem: the import writes its digit matrices too
+      if ((digit_sides >> side) & 1) {  // tensor-core problem: the import writes the digit matrices it reads
         j.digits = g->ctxs[p]->digits[side];
         tc_digit_table(m, j.dtab);
       }
+      if ((digit_sides >> (2 + side)) & 1) j.nibbles = g->ctxs[p]->nibbles[side];  // ... and nibble matrices
       j.warp0 = warps;
       warps += m.nrows_a * j.segs;
       jobs.push_back(j);
@@ -160,11 +163,26 @@ cudaError_t enqueue_gemm(gbs_group *g, cudaStream_t s) {
   return e;
 }
 
-// True when some tensor-core problem's digit matrices are older than its planes.
+// True when a digit or nibble matrix some tensor-core problem reads is older than its planes.
 bool digits_stale(const gbs_group *g) {
-  for (const gbs_ctx *c : g->tc.ctxs)
-    if (!c->digits_valid[0] || !c->digits_valid[1]) return true;
+  for (size_t i = 0; i < g->tc.ctxs.size(); i++)
+    for (int side = 0; side < 2; side++) {
+      if (((g->tc.sides[i] >> side) & 1) && !g->tc.ctxs[i]->digits_valid[side]) return true;
+      if (((g->tc.sides[i] >> (2 + side)) & 1) && !g->tc.ctxs[i]->nibbles_valid[side]) return true;
+    }
   return false;
+}
+
+// After a grouped pack: the digit and nibble matrices it wrote match the new
+// planes, any other of the group's contexts is stale.
+void mark_packed_digits(const gbs_group *g) {
+  for (gbs_ctx *c : g->ctxs)
+    for (int side = 0; side < 2; side++) c->digits_valid[side] = c->nibbles_valid[side] = false;
+  for (size_t i = 0; i < g->tc.ctxs.size(); i++)
+    for (int side = 0; side < 2; side++) {
+      g->tc.ctxs[i]->digits_valid[side] = ((g->tc.sides[i] >> side) & 1) != 0;
+      g->tc.ctxs[i]->nibbles_valid[side] = ((g->tc.sides[i] >> (2 + side)) & 1) != 0;
+    }
 }
 
 // 0 = per-problem choice, 1 = popcount kernel only, 2 = tensor-core kernel wherever exact.
@@ -340,7 +358,7 @@ int gbs_group_import(gbs_group *g, const void *const *lhs_srcs, const void *cons
     c->lhs.imported = c->rhs.imported = true;
     c->vt_valid[0] = c->vt_valid[1] = false;
   }
-  for (gbs_ctx *c : g->tc.ctxs) c->digits_valid[0] = c->digits_valid[1] = true;  // written by the pack
+  mark_packed_digits(g);
   return GBS_OK;
 }
 
@@ -393,7 +411,7 @@ int gbs_group_capture(gbs_group *g, const void *const *lhs_srcs, const void *con
                            (g->tc.ntiles ? 1 : 0);
   if (with_pack) {
     for (gbs_ctx *c : g->ctxs) c->lhs.imported = c->rhs.imported = true;
-    for (gbs_ctx *c : g->tc.ctxs) c->digits_valid[0] = c->digits_valid[1] = true;  // each replay packs them
+    mark_packed_digits(g);  // each replay packs them
   }
   return GBS_OK;
 }
@@ -402,8 +420,10 @@ int gbs_group_replay(gbs_group *g, void *stream) {
   if (!g || !g->exec) return fail(GBS_ESTATE, "gbs_group_replay: capture the group first");
   cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "gbs_group_replay");
-  if (g->npack)  // the replay packs new planes: cached adjoint operands are stale
+  if (g->npack) {  // the replay packs new planes: cached adjoint operands and other derived copies are stale
     for (gbs_ctx *c : g->ctxs) c->vt_valid[0] = c->vt_valid[1] = false;
+    mark_packed_digits(g);
+  }
   for (gbs_ctx *c : g->ctxs) c->res_stale = false;
   count_launch(g->launches_per_replay);
   return GBS_OK;
@@ -437,6 +457,12 @@ int gbs_group_split(const gbs_group *g, uint64_t *popc_problems, uint64_t *tc_pr
   if (tc_problems) *tc_problems = g->tc.ctxs.size();
   if (tc_tiles) *tc_tiles = g->tc.ntiles;
   return GBS_OK;
+}
+
+int gbs_debug_group_tc_kernel(const gbs_group *g) {
+  if (!g) return fail(GBS_EINVAL, "gbs_debug_group_tc_kernel: group is NULL");
+  if (!g->tc.ntiles) return 0;
+  return g->tc.nibbles ? 2 : 1;
 }
 
 int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile) {

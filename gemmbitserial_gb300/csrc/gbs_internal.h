@@ -29,6 +29,13 @@ constexpr int kMaxBits = 8;
 __host__ __device__ inline uint64_t digit_offset(uint64_t r, uint64_t col, uint64_t ncols_a) {
   return ((r >> 4) * (ncols_a >> 7) + (col >> 7)) * 2048 + ((r & 15) << 7) + (col & 127);
 }
+// The nibble matrix (the tensor-core pipe's compact copy of an operand: each
+// element's plane code in 4 bits, the even column in the low nibble) has the
+// same blocks at half the bytes: [rows/16][cols/128][16][64].  Byte offset
+// of the code pair holding column col (col even).
+__host__ __device__ inline uint64_t nibble_offset(uint64_t r, uint64_t col, uint64_t ncols_a) {
+  return ((r >> 4) * (ncols_a >> 7) + (col >> 7)) * 1024 + ((r & 15) << 6) + ((col & 127) >> 1);
+}
 
 // One bit-serial matrix on the device: planes [nbits][nrows_a][wpr] of u64,
 // with the reference's nrows_a and ncols_a (BitSerialMatrix, gemmbitserial.hpp:
@@ -95,6 +102,7 @@ struct PackJob {
   uint64_t *planes;
   int32_t *rowsum;
   uint8_t *digits;
+  uint8_t *nibbles;  // with nibbles set, the import also writes the nibble matrix (codes, 4 bits each)
   uint64_t nrows, ncols, nrows_a, wpr, warp0;
   uint64_t dcols;  // digit-matrix columns (a multiple of 256)
   int nbits, issigned, dtype, vec;
@@ -102,17 +110,23 @@ struct PackJob {
   uint32_t dtab[4];
 };
 
-// One problem of the persistent tensor-core kernel (device resident).  The
+// One problem of the persistent tensor-core kernels (device resident).  The
 // MMA's row operand ("MMA-A", 128 rows per tile) is the lhs, or the rhs when
-// swap is set; the other operand gives the MMA's N = bn columns per tile.
+// swap is set; the other operand gives the MMA's N columns per tile.  The
+// digit kernel (gbs_gemm_tcg.cu) takes the larger side as MMA-A and reads
+// both operands' digit matrices, N = bn; the nibble kernel
+// (gbs_gemm_tcgn.cu) takes the smaller side as MMA-A (digits) and decodes
+// the larger from its nibble matrix, N = 256.
 struct TcgProblem {
   int32_t *C;               // result [N][M]
   uint32_t M, N;
-  uint32_t a_rows, b_rows;  // padded rows of the MMA-A / MMA-B digit matrices
+  uint32_t a_rows, b_rows;  // padded rows of the MMA-A digit matrix / the MMA-B digit (nibble) matrix
   uint32_t nk;              // K stages of 128 digits
-  uint32_t bn;              // MMA N: a multiple of 16 in [16, 256]
-  uint32_t idesc;           // tcgen05 instruction descriptor for M = 128, N = bn
+  uint32_t bn;              // digit kernel: MMA N, a multiple of 16 in [16, 256]
+  uint32_t idesc;           // tcgen05 instruction descriptor for M = 128 and the kernel's N
   uint32_t swap;            // 1: MMA-A = rhs (tile rows are n), MMA-B = lhs (columns are m)
+  uint32_t w4;              // nibble kernel: MMA-B codes of 4 bits (the two-table lookup)
+  uint32_t tab[4];          // nibble kernel: e4m3 byte of every MMA-B code
 };
 
 // One output tile: problem, 128-row block of MMA-A, bn-column block of MMA-B.
@@ -120,19 +134,27 @@ struct TcgTile {
   uint32_t p, r, c, pad;
 };
 
-// One operand of a digit expansion pass (planes -> e4m3 digit matrix).
+// One operand of an expansion pass: planes -> e4m3 digit matrix, or planes
+// -> nibble matrix (nib set: the plane codes, 4 bits each).
 struct ExpandJob {
   const uint64_t *planes;
-  uint8_t *digits;
+  uint8_t *digits;   // the digit or nibble matrix
   uint64_t nrows_a, wpr, dcols;  // plane rows and words per row; digit-matrix columns
-  uint64_t thread0;  // first global thread of this job (16 digits per thread)
+  uint64_t thread0;  // first global thread of this job (16 digits or 32 codes per thread)
   uint32_t nrows, K, chunks, nbits;
   uint32_t tab[4];   // e4m3 byte of every plane code, 4 per word
+  uint32_t nib;
 };
 
-// Host-side plan of the persistent tensor-core kernel over some contexts.
+// Host-side plan of the persistent tensor-core kernels over some contexts.
 struct TcgPlan {
   std::vector<gbs_ctx *> ctxs;
+  // derived matrices each context needs: bit 0 / 1 the lhs / rhs digit
+  // matrix, bit 2 / 3 the lhs / rhs nibble matrix (both digit matrices for
+  // the digit kernel; the smaller side's digits and the larger side's
+  // nibbles for the nibble kernel)
+  std::vector<uint8_t> sides;
+  bool nibbles = false;  // the nibble kernel (gbs_gemm_tcgn.cu) runs the plan
   TcgProblem *d_probs = nullptr;
   void *d_maps = nullptr;  // CUtensorMap [2 * nprob]: MMA-A map, MMA-B map of each problem
   TcgTile *d_tiles = nullptr;
@@ -186,6 +208,10 @@ struct gbs_ctx {
   // pipe's operands), built from the planes on first use after each import
   uint8_t *digits[2] = {nullptr, nullptr};
   bool digits_valid[2] = {false, false};
+  // nibble matrices [drows][dcols / 2] (4-bit plane codes) of either side, the
+  // larger operand's form for the nibble kernel, built like the digits
+  uint8_t *nibbles[2] = {nullptr, nullptr};
+  bool nibbles_valid[2] = {false, false};
   alignas(64) unsigned char tc_map_da[128];
   alignas(64) unsigned char tc_map_db[128];
   bool digit_maps_ready = false;
@@ -281,6 +307,11 @@ void tcg_plan_free(TcgPlan *plan);
 cudaError_t tcg_expand(TcgPlan &plan, cudaStream_t s);
 cudaError_t tcg_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s, int32_t *out0 = nullptr);
 cudaError_t ensure_digit_buffer(gbs_ctx *c, int side);
+cudaError_t ensure_nibble_buffer(gbs_ctx *c, int side);
+// the nibble kernel over a plan built with nibbles set (gbs_gemm_tcgn.cu)
+cudaError_t tcgn_gemm(const TcgPlan &plan, uint32_t *err, cudaStream_t s, int32_t *out0);
+cudaError_t tcgn_prepare();  // kernel attributes, once per plan build
+bool tc_map_nibbles(void *map, const uint8_t *base, uint64_t cols, uint64_t rows);
 // tensor-core pipe for 5-8-bit operands (gbs_wide.cu): operands split into parts of <= 4 bits
 bool tc_wide(const gbs_ctx *c);
 cudaError_t launch_gemm_wide(gbs_ctx *c, cudaStream_t s, int variant);
@@ -290,6 +321,7 @@ int adjoint_tc(gbs_ctx *c, const float *dC, float *dA, float *dB, cudaStream_t s
 bool adjoint_tc_available();
 void adj_plan_free(AdjPlan *p);
 ExpandJob make_expand_job(const Mat &m, uint8_t *digits);
+ExpandJob make_nibble_job(const Mat &m, uint8_t *nibbles);
 cudaError_t launch_expand(const ExpandJob &job, cudaStream_t s);
 int effective_pipe(const gbs_ctx *c);
 int tuned_variant(const gbs_ctx *c, int pipe);

@@ -139,6 +139,24 @@ __device__ __forceinline__ void write_digits32(uint8_t *__restrict__ digits, int
   dst[1] = make_uint4(d[4], d[5], d[6], d[7]);
 }
 
+// The lane's 32 codes of row r < nrows into the nibble matrix (dcols columns,
+// blocks of nibble_offset): the low nbits bits of each code byte, two codes a
+// byte (even column low).  Codes past ncols are whatever the source gave:
+// the tensor-core kernel multiplies them by digits that are zero there.
+__device__ __forceinline__ void write_nibbles32(uint8_t *__restrict__ nib, int nbits, uint64_t dcols, uint64_t r,
+                                                uint64_t col0, const uint32_t (&q)[8]) {
+  const uint32_t msk = 0x01010101u * ((1u << nbits) - 1u);
+  uint32_t o[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    uint32_t t0 = q[2 * i] & msk, t1 = q[2 * i + 1] & msk;
+    t0 |= t0 >> 4;  // bytes 0 and 2: code pairs
+    t1 |= t1 >> 4;
+    o[i] = __byte_perm(t0, t1, 0x6420u);
+  }
+  *reinterpret_cast<uint4 *>(nib + nibble_offset(r, col0, dcols)) = make_uint4(o[0], o[1], o[2], o[3]);
+}
+
 // One 1024-column unit: codes, planes and (optionally) digits of the lane's 32 columns.
 __device__ __forceinline__ void pack_unit(const void *__restrict__ src, int dtype, int bipolar, int issigned,
                                           int nbits,
@@ -304,6 +322,7 @@ __global__ void __launch_bounds__(256) pack_grouped(const PackJob *__restrict__ 
           const uint4 tab = make_uint4(J.dtab[0], J.dtab[1], J.dtab[2], J.dtab[3]);
           write_digits32(J.digits, J.nbits, J.nrows, J.ncols, J.dcols, tab, rc, col0, q);
         }
+        if (J.nibbles && rc < J.nrows) write_nibbles32(J.nibbles, J.nbits, J.dcols, rc, col0, q);
       }
       if (w + 1 < last) {
         jc = jn;

@@ -149,6 +149,8 @@ void wide_plan_free(WidePlan *p) {
       }
       if (s->sk_ws) cudaFree(s->sk_ws);
       if (s->sk_flags) cudaFree(s->sk_flags);
+      for (uint8_t *nb : s->nibbles)
+        if (nb) cudaFree(nb);
       delete s;  // its planes alias the parent's, its digit matrices are the plan's
     }
   for (auto &side : p->digits)
@@ -166,6 +168,9 @@ cudaError_t launch_gemm_wide(gbs_ctx *c, cudaStream_t s, int variant) {
   const Mat *side_m[2] = {&c->lhs, &c->rhs};
   for (int side = 0; side < 2; side++) {
     if (c->digits_valid[side]) continue;
+    for (auto &row : p.sub)  // the parts' own nibble matrices (one-problem plans) are stale too
+      for (gbs_ctx *sub : row)
+        if (sub) sub->nibbles_valid[side] = false;
     for (int k = 0; k < p.parts[side]; k++) {
       cudaError_t e = launch_expand(make_expand_job(part_of(*side_m[side], k), p.digits[side][k]), s);
       if (e != cudaSuccess) return e;

@@ -63,7 +63,8 @@ class Group:
         d, e, f = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _capi.check(_capi.load().gbs_group_split(self._h, C.byref(d), C.byref(e), C.byref(f)))
         return {"tiles": a.value, "smem_bytes": b.value, "grid": c.value,
-                "popc_problems": d.value, "tc_problems": e.value, "tc_tiles": f.value}
+                "popc_problems": d.value, "tc_problems": e.value, "tc_tiles": f.value,
+                "tc_kernel": ("none", "digits", "nibbles")[_capi.load().gbs_debug_group_tc_kernel(self._h)]}
 
     def free(self):
         if self._h:

@@ -369,6 +369,13 @@ GBS_API uint32_t gbs_debug_tc_error(void);
  * exercise the grouped kernel's descriptor validation (host-side injection). */
 GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 
+/* Which persistent tensor-core kernel runs a group's tensor-core problems:
+ * 0 none, 1 the digit kernel (both operands as e4m3 digit matrices), 2 the
+ * nibble kernel (the larger operand as 4-bit codes, decoded to digits in
+ * shared memory).  GBS_TCG_NIBBLES=0 in the environment at gbs_group_create
+ * keeps a group on the digit kernel.  Negative on a NULL group. */
+GBS_API int gbs_debug_group_tc_kernel(const gbs_group *g);
+
 /* Exercises the tensor-core kernels' bounded waits without a GPU fault: one
  * launch of the SM-pair kernel over ctx (an imported context of M, N >= 256
  * whose widths the tensor cores cover) that loads and multiplies nothing, so

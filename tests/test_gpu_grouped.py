@@ -26,13 +26,18 @@ def make_contexts(mix):
     return [allocGEMMContext(M, K, N, wA, wB, eA != "u", eB != "u") for (M, K, N, wA, eA, wB, eB) in mix]
 
 
-@pytest.fixture(params=["auto", "tc", "popc"])
+@pytest.fixture(params=["auto", "tc", "tc-digits", "popc"])
 def group_pipe(request, monkeypatch):
-    """GBS_GROUP_PIPE as read by gbs_group_create: per-problem choice, or one kernel forced."""
+    """GBS_GROUP_PIPE as read by gbs_group_create: per-problem choice, or one kernel forced;
+    tc-digits also keeps the tensor-core problems on the digit kernel (GBS_TCG_NIBBLES=0)
+    instead of the nibble kernel."""
+    monkeypatch.delenv("GBS_TCG_NIBBLES", raising=False)
     if request.param == "auto":
         monkeypatch.delenv("GBS_GROUP_PIPE", raising=False)
     else:
-        monkeypatch.setenv("GBS_GROUP_PIPE", request.param)
+        monkeypatch.setenv("GBS_GROUP_PIPE", request.param.split("-")[0])
+    if request.param == "tc-digits":
+        monkeypatch.setenv("GBS_TCG_NIBBLES", "0")
     return request.param
 
 
@@ -41,8 +46,10 @@ def check_split(g, mode, count):
     assert st["popc_problems"] + st["tc_problems"] == count
     if mode == "popc":
         assert st["tc_problems"] == 0
-    if mode == "tc":
+        assert st["tc_kernel"] == "none"
+    if mode.startswith("tc"):
         assert st["tc_problems"] > 0
+        assert st["tc_kernel"] == ("digits" if mode == "tc-digits" else "nibbles")
     return st
 
 
@@ -102,6 +109,14 @@ EDGE_MIX = [
     (64, 74565, 96, 4, "u", 4, "u"),     # 74565 * 15 * 15 < 2^24
     (96, 512, 48, 2, "s", 4, "s"),
     (200, 129, 1, 2, "u", 2, "u"),
+    # the nibble kernel's larger operand of every width and encoding, odd words per
+    # row, several 256-row column tiles, and K at the fp32 exactness limit
+    (333, 960, 40, 3, "s", 2, "u"),      # wpr 15
+    (5, 1088, 777, 1, "u", 3, "s"),      # wpr 17
+    (9, 1472, 391, 2, "u", 1, "b"),      # wpr 23, bipolar row operand
+    (41, 4992, 300, 3, "u", 1, "u"),
+    (40, 74560, 130, 4, "u", 3, "u"),    # wpr 1165
+    (40, 80000, 130, 4, "u", 3, "u"),    # 80000 * 15 * 7 < 2^24
 ]
 
 
@@ -115,7 +130,7 @@ def test_grouped_tc_edge_shapes(group_pipe):
     g = Group(ctxs)
     try:
         st = check_split(g, group_pipe, len(EDGE_MIX))
-        if group_pipe == "tc":
+        if group_pipe.startswith("tc"):
             assert st["tc_problems"] == len(EDGE_MIX)
         g.import_([a for a, _ in dev], [b for _, b in dev])
         g.gemm()
