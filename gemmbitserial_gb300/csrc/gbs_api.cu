@@ -710,11 +710,12 @@ int gbs_clear(gbs_ctx *c, int side, void *stream) {
 
 int gbs_set_variant(gbs_ctx *c, int variant) {
   if (!c) return fail(GBS_EINVAL, "gbs_set_variant: ctx is NULL");
-  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == 128 || variant == 256 || variant == kPairVariant ||
+  if (!(variant == -1 || (variant >= 0 && variant <= 2) || variant == kRowsCls || variant == 128 || variant == 256 ||
+        variant == kPairVariant ||
         variant == kPairVariant128 || variant == kPairVariantPersistent || variant == kPairVariantStreamK ||
         pair_split_variant(variant)))
     return fail(GBS_EINVAL,
-                "gbs_set_variant: variant must be -1, 0..2, 128, 256, 512..515, 1281, 1282, 1284, 2561, 2562 or 2564");
+                "gbs_set_variant: variant must be -1, 0..2, 4, 128, 256, 512..515, 1281, 1282, 1284, 2561, 2562 or 2564");
   c->variant = variant;
   return GBS_OK;
 }
@@ -759,7 +760,9 @@ int gbs_gemm(gbs_ctx *c, void *stream) {
   sh.wa = (int)c->lhs.nbits;
   sh.wb = (int)c->rhs.nbits;
   const int variant = c->variant >= 0 ? c->variant : (c->pipe == GBS_PIPE_AUTO ? tuned_variant(c, pipe) : -1);
-  sh.tile_cls = (pipe == GBS_PIPE_POPC && variant >= 0 && variant <= 2) ? variant : -1;
+  sh.tile_cls = (pipe == GBS_PIPE_POPC && ((variant >= 0 && variant <= 2) || (variant == kRowsCls && M <= kRowsMaxM)))
+                    ? variant
+                    : -1;
   cudaError_t ke;
   if (pipe == GBS_PIPE_TC && tc_wide(c)) {
     ke = launch_gemm_wide(c, s, variant);

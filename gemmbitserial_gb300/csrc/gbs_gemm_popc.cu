@@ -15,8 +15,12 @@
 //    (double buffered).  Thread (tx, ty) owns lhs rows tx + (BM/4)i and rhs
 //    rows ty + (BN/4)j, so consecutive lanes store consecutive results of the
 //    transposed output row.
+//  * gemm_popc_rows: for at most 16 lhs rows, every lhs row x 256 rhs rows
+//    per CTA, one rhs row per thread (popcounts only on real lhs rows, up to
+//    the next power of two).
 //  * gemm_popc_grouped: persistent; CTAs pull tiles of many independent
-//    problems from a device queue (atomic counter) and run the same tile code.
+//    problems from a device queue (atomic counter) and run the same tile code
+//    (the three BM x BN classes, the rows tile, or the skinny class).
 //  * gemm_popc_skinny: one warp per output element, lanes stride over the K
 //    words; for matrix-vector and other small-output shapes.
 #include "gbs_internal.h"
@@ -176,30 +180,180 @@ __device__ __forceinline__ void popc_tile(const TileArgs &g, uint64_t m0, uint64
   }
 }
 
+// The rows tile: every lhs row of a problem with at most MB (<= 16) of them x
+// NT rhs rows.  Thread t owns rhs row n0 + t and its M outputs, so popcounts
+// are spent on at most the next power of two of M lhs rows instead of a
+// 16- or 32-row tile's padding (for M = 1 the BM x BN classes do 16x the
+// work).  The pipeline steps over (rhs plane j, K chunk) pairs: a stage holds
+// one K chunk of rhs plane j for the NT rows and of every lhs plane for the
+// 16 staged lhs rows, so its shared memory does not grow with wb.  The lhs
+// words are read as broadcasts.  Ends with a __syncthreads().
+constexpr int kRowsStagedRows = kRowsMaxM;
+__host__ __device__ constexpr size_t rows_stage_words(int wa, int kc) {
+  return (size_t)(wa * kRowsStagedRows + NT) * (kc + 2);
+}
+
+template <int MB, int KC, bool XOR>
+__device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, uint64_t *smem) {
+  constexpr int LDW = KC + 2;
+  const int wa = g.wa, wb = g.wb, tid = threadIdx.x;
+  const int stage_words = (int)rows_stage_words(wa, KC);
+  const uint64_t wpr = g.wpr;
+  const int nchunks = (int)((wpr + KC - 1) / KC);
+  const int nsteps = nchunks * wb;
+
+  auto load_stage = [&](int st, int step) {
+    const int j = step / nchunks;
+    const uint64_t k0 = (uint64_t)(step % nchunks) * KC;
+    uint64_t *s = smem + st * stage_words;
+    const int a_rows = wa * kRowsStagedRows;
+    const int piece = (wpr & 1) ? 1 : 2;  // odd word counts (64-bit column padding): 8-byte pieces
+    const int per_row = KC / piece, all = (a_rows + NT) * per_row;
+    for (int idx = tid; idx < all; idx += NT) {
+      const int row = idx / per_row, p = idx % per_row;
+      const bool isA = row < a_rows;
+      const uint64_t k = k0 + (uint64_t)(p * piece);
+      const uint64_t *base;
+      uint64_t grow;
+      bool ok;
+      if (isA) {
+        const int plane = row / kRowsStagedRows, r = row % kRowsStagedRows;
+        base = g.A + plane * g.a_plane;
+        grow = (uint64_t)r;
+        ok = k < wpr && grow < g.a_rows;
+      } else {
+        base = g.B + j * g.b_plane;
+        grow = n0 + (uint64_t)(row - a_rows);
+        ok = k < wpr && grow < g.b_rows;
+      }
+      uint64_t *dst = s + row * LDW + p * piece;
+      if (piece == 2) cp_async16(dst, ok ? base + grow * wpr + k : base, ok);
+      else cp_async8(dst, ok ? base + grow * wpr + k : base, ok);
+    }
+  };
+
+  uint32_t acc[MB];
+#pragma unroll
+  for (int m = 0; m < MB; m++) acc[m] = 0u;
+
+  if (nsteps > 0) {
+    load_stage(0, 0);
+    cp_commit();
+  }
+  for (int st = 0; st < nsteps; st++) {
+    if (st + 1 < nsteps) {
+      load_stage((st + 1) & 1, st + 1);
+      cp_commit();
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+    const int j = st / nchunks;
+    const uint64_t *sa = smem + (st & 1) * stage_words;
+    const uint64_t *pb = sa + (wa * kRowsStagedRows + tid) * LDW;
+#pragma unroll 1
+    for (int i = 0; i < wa; i++) {
+      const uint64_t *pa = sa + i * kRowsStagedRows * LDW;
+      const uint32_t al = alpha_of(i, j, g.neg_i, g.neg_j, g.shift, XOR);  // weights fold in per count (mod 2^32)
+      constexpr int kUnroll = MB >= 8 ? 1 : 8 / MB;  // about 8 independent counts per unrolled step
+#pragma unroll kUnroll
+      for (int kp = 0; kp < KC / 2; kp++) {
+        const ulonglong2 b = *reinterpret_cast<const ulonglong2 *>(pb + 2 * kp);
+#pragma unroll
+        for (int m = 0; m < MB; m++)
+          acc[m] += pc2<XOR>(*reinterpret_cast<const ulonglong2 *>(pa + m * LDW + 2 * kp), b) * al;
+      }
+    }
+    __syncthreads();
+  }
+
+  const uint64_t gn = n0 + tid;
+  if (gn < g.N) {
+    const uint32_t bn = g.c0 - (g.rb ? (uint32_t)g.rb[gn] : 0u);
+#pragma unroll
+    for (int m = 0; m < MB; m++)
+      if (m < (int)g.M) g.C[gn * g.M + m] = (int32_t)(acc[m] + bn - (g.ra ? (uint32_t)g.ra[m] : 0u));
+  }
+}
+
+template <int KC, bool XOR>
+__device__ __forceinline__ void popc_rows_dispatch(const TileArgs &g, uint64_t n0, uint64_t *smem) {
+  if (g.M <= 1) popc_rows_tile<1, KC, XOR>(g, n0, smem);
+  else if (g.M <= 2) popc_rows_tile<2, KC, XOR>(g, n0, smem);
+  else if (g.M <= 4) popc_rows_tile<4, KC, XOR>(g, n0, smem);
+  else if (g.M <= 8) popc_rows_tile<8, KC, XOR>(g, n0, smem);
+  else popc_rows_tile<16, KC, XOR>(g, n0, smem);
+}
+
+template <bool XOR>
+__global__ void __launch_bounds__(NT, 2) gemm_popc_rows(TileArgs g) {
+  extern __shared__ __align__(16) uint64_t smem[];
+  popc_rows_dispatch<kRowsKC, XOR>(g, (uint64_t)blockIdx.x * NT, smem);
+}
+
 template <int BM, int BN, int KC, bool XOR>
 __global__ void __launch_bounds__(NT, 2) gemm_popc_tiled(TileArgs g) {
   extern __shared__ __align__(16) uint64_t smem[];
   popc_tile<BM, BN, KC, XOR>(g, (uint64_t)blockIdx.x * BM, (uint64_t)blockIdx.y * BN, smem);
 }
 
+// One output's weighted popcounts over every plane pair, this lane's share:
+// words lane, lane + 32, ... of lhs row a0 and rhs row b0 (planes a_plane /
+// b_plane words apart).  Each step loads U x 32 words of every plane first --
+// independent loads, one memory latency per step rather than one per plane
+// pair and 32 words -- then counts.  WM >= max(wa, wb) sizes the register
+// arrays.  Words past wpr count as zero (AND and XOR alike).
+template <int WM, int U, typename Alpha>
+__device__ __forceinline__ uint32_t skinny_lane_sum_t(const uint64_t *__restrict__ a0, uint64_t a_plane,
+                                                      const uint64_t *__restrict__ b0, uint64_t b_plane, uint64_t wpr,
+                                                      int wa, int wb, bool use_xor, int lane, Alpha alpha) {
+  uint32_t acc = 0;
+  for (uint64_t w0 = 0; w0 < wpr; w0 += 32 * U) {
+    uint64_t av[WM][U], bv[WM][U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const uint64_t w = w0 + (uint64_t)(32 * u + lane);
+      const bool in = w < wpr;
+#pragma unroll
+      for (int i = 0; i < WM; i++) av[i][u] = (in && i < wa) ? __ldg(a0 + i * a_plane + w) : 0ull;
+#pragma unroll
+      for (int j = 0; j < WM; j++) bv[j][u] = (in && j < wb) ? __ldg(b0 + j * b_plane + w) : 0ull;
+    }
+#pragma unroll
+    for (int i = 0; i < WM; i++) {
+      if (i >= wa) break;
+#pragma unroll
+      for (int j = 0; j < WM; j++) {
+        if (j >= wb) break;
+        uint32_t c = 0;
+#pragma unroll
+        for (int u = 0; u < U; u++) c += (uint32_t)(use_xor ? __popcll(av[i][u] ^ bv[j][u]) : __popcll(av[i][u] & bv[j][u]));
+        acc += c * alpha(i, j);
+      }
+    }
+  }
+  return acc;
+}
+
+template <typename Alpha>
+__device__ __forceinline__ uint32_t skinny_lane_sum(const uint64_t *__restrict__ a0, uint64_t a_plane,
+                                                    const uint64_t *__restrict__ b0, uint64_t b_plane, uint64_t wpr,
+                                                    int wa, int wb, bool use_xor, int lane, Alpha alpha) {
+  const int wm = wa > wb ? wa : wb;
+  if (wm <= 1) return skinny_lane_sum_t<1, 4>(a0, a_plane, b0, b_plane, wpr, wa, wb, use_xor, lane, alpha);
+  if (wm <= 2) return skinny_lane_sum_t<2, 4>(a0, a_plane, b0, b_plane, wpr, wa, wb, use_xor, lane, alpha);
+  if (wm <= 4) return skinny_lane_sum_t<4, 2>(a0, a_plane, b0, b_plane, wpr, wa, wb, use_xor, lane, alpha);
+  return skinny_lane_sum_t<kMaxBits, 1>(a0, a_plane, b0, b_plane, wpr, wa, wb, use_xor, lane, alpha);
+}
+
 // One output (m, n) of a grouped problem by one warp, lanes over the K words
 // (the skinny tile class: matrix-vector and other small-output problems).
 __device__ __forceinline__ void grouped_skinny_output(const GroupProblem &P, uint64_t o, int lane) {
   const uint64_t n = o / P.M, m = o % P.M;
-  uint32_t acc = 0;
-  for (int i = 0; i < P.wa; i++) {
-    const uint64_t *a = P.A + i * P.a_plane + m * P.wpr;
-    for (int j = 0; j < P.wb; j++) {
-      const uint64_t *b = P.B + j * P.b_plane + n * P.wpr;
-      uint32_t cnt = 0;
-      if (P.use_xor) {
-        for (uint64_t w = lane; w < P.wpr; w += 32) cnt += __popcll(a[w] ^ b[w]);
-      } else {
-        for (uint64_t w = lane; w < P.wpr; w += 32) cnt += __popcll(a[w] & b[w]);
-      }
-      acc += cnt * alpha_of(i, j, P.neg_i, P.neg_j, P.shift, P.use_xor);
-    }
-  }
+  uint32_t acc = skinny_lane_sum(P.A + m * P.wpr, P.a_plane, P.B + n * P.wpr, P.b_plane, P.wpr, P.wa, P.wb,
+                                 P.use_xor != 0, lane,
+                                 [&](int i, int j) { return alpha_of(i, j, P.neg_i, P.neg_j, P.shift, P.use_xor); });
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
   if (lane == 0) {
@@ -224,7 +378,7 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *_
     __syncthreads();
     if (t >= ntiles) break;
     const GroupTile tl = tiles[t];
-    if (tl.p >= (uint32_t)nprob || tl.cls > kSkinnyCls) {
+    if (tl.p >= (uint32_t)nprob || tl.cls > kRowsCls) {
       if (threadIdx.x == 0) atomicOr(err, 1u);
       continue;
     }
@@ -239,9 +393,11 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *_
       if (o < P.M * P.N) grouped_skinny_output(P, o, threadIdx.x & 31);
       continue;
     }
-    const int bm = tile_bm((int)tl.cls), bn = tile_bn((int)tl.cls);
+    const bool rows = tl.cls == kRowsCls;
+    const int bm = rows ? kRowsMaxM : tile_bm((int)tl.cls), bn = rows ? NT : tile_bn((int)tl.cls);
     const uint64_t m0 = (uint64_t)tl.mt * bm, n0 = (uint64_t)tl.nt * bn;
-    if (m0 >= P.M || n0 >= P.N || P.wa < 1 || P.wa > kMaxBits || P.wb < 1 || P.wb > kMaxBits) {
+    if (m0 >= P.M || n0 >= P.N || P.wa < 1 || P.wa > kMaxBits || P.wb < 1 || P.wb > kMaxBits ||
+        (rows && P.M > (uint64_t)kRowsMaxM)) {
       if (threadIdx.x == 0) atomicOr(err, 2u);
       continue;
     }
@@ -250,7 +406,10 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *_
     g.M = P.M; g.N = P.N; g.wpr = P.wpr; g.a_plane = P.a_plane; g.b_plane = P.b_plane;
     g.a_rows = P.a_rows; g.b_rows = P.b_rows;
     g.wa = P.wa; g.wb = P.wb; g.neg_i = P.neg_i; g.neg_j = P.neg_j; g.shift = P.shift; g.c0 = P.c0;
-    if (P.use_xor) {
+    if (rows) {
+      if (P.use_xor) popc_rows_dispatch<kRowsKC, true>(g, n0, smem);
+      else popc_rows_dispatch<kRowsKC, false>(g, n0, smem);
+    } else if (P.use_xor) {
       if (tl.cls == 0) popc_tile<64, 64, kGroupKC, true>(g, m0, n0, smem);
       else if (tl.cls == 1) popc_tile<32, 128, kGroupKC, true>(g, m0, n0, smem);
       else popc_tile<16, 256, kGroupKC, true>(g, m0, n0, smem);
@@ -268,20 +427,8 @@ __global__ void __launch_bounds__(256) gemm_popc_skinny(GemmShape g, Epilogue e)
   const int lane = threadIdx.x & 31;
   if (o >= g.M * g.N) return;  // warp-uniform
   const uint64_t n = o / g.M, m = o % g.M;
-  uint32_t acc = 0;
-  for (int i = 0; i < g.wa; i++) {
-    const uint64_t *a = g.A + i * g.a_plane + m * g.wpr;
-    for (int j = 0; j < g.wb; j++) {
-      const uint64_t *b = g.B + j * g.b_plane + n * g.wpr;
-      uint32_t cnt = 0;
-      if (e.use_xor) {
-        for (uint64_t w = lane; w < g.wpr; w += 32) cnt += __popcll(a[w] ^ b[w]);
-      } else {
-        for (uint64_t w = lane; w < g.wpr; w += 32) cnt += __popcll(a[w] & b[w]);
-      }
-      acc += cnt * (uint32_t)e.alpha[i][j];
-    }
-  }
+  uint32_t acc = skinny_lane_sum(g.A + m * g.wpr, g.a_plane, g.B + n * g.wpr, g.b_plane, g.wpr, g.wa, g.wb,
+                                 e.use_xor != 0, lane, [&](int i, int j) { return (uint32_t)e.alpha[i][j]; });
 #pragma unroll
   for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
   if (lane == 0) {
@@ -317,7 +464,20 @@ cudaError_t run_tiled_cls(int cls, const TileArgs &t, cudaStream_t s) {
   return run_tiled_kc<64, 64, XOR>(t, s);
 }
 
+template <bool XOR>
+cudaError_t run_rows(const TileArgs &t, cudaStream_t s) {
+  const size_t smem = popc_rows_smem(t.wa, kRowsKC);
+  auto kern = gemm_popc_rows<XOR>;
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  kern<<<(unsigned)((t.N + NT - 1) / NT), NT, smem, s>>>(t);
+  count_launch();
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+size_t popc_rows_smem(int wa, int kc) { return 2 * rows_stage_words(wa, kc) * sizeof(uint64_t); }
 
 size_t popc_stage_smem(int cls, int wa, int wb, int kc) {
   return 2ull * (wa * tile_bm(cls) + wb * tile_bn(cls)) * (kc + 2) * sizeof(uint64_t);
@@ -347,6 +507,9 @@ cudaError_t launch_gemm_popc(const GemmShape &g, const Epilogue &e, cudaStream_t
   t.M = g.M; t.N = g.N; t.wpr = g.wpr; t.a_plane = g.a_plane; t.b_plane = g.b_plane;
   t.a_rows = g.a_rows; t.b_rows = g.b_rows;
   t.wa = g.wa; t.wb = g.wb; t.neg_i = e.neg_i; t.neg_j = e.neg_j; t.shift = e.shift; t.c0 = e.c0;
+  // at most 16 lhs rows: the rows tile (no popcounts on padding rows), unless a class is forced
+  if (g.tile_cls == kRowsCls || (g.tile_cls < 0 && g.M <= (uint64_t)kRowsMaxM))
+    return e.use_xor ? run_rows<true>(t, s) : run_rows<false>(t, s);
   const int cls = (g.tile_cls >= 0 && g.tile_cls <= 2) ? g.tile_cls : popc_tile_class(g.M, g.wa, g.wb, 220 * 1024);
   if (e.use_xor) return run_tiled_cls<true>(cls, t, s);
   return run_tiled_cls<false>(cls, t, s);

@@ -28,6 +28,7 @@
 // Every mbarrier wait is bounded; on timeout the CTA sets a bit in the
 // caller's error word, stops issuing, drains what it issued and frees TMEM.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -430,18 +431,63 @@ void tcg_plan_free(TcgPlan *p) {
 
 namespace {
 
-// GBS_TCG_NIBBLES=0 in the environment keeps the plans built from then on on
-// the digit kernel.
-bool nibbles_enabled() {
+// GBS_TCG_NIBBLES in the environment when a plan is built: 0 keeps it on the
+// digit kernel, 1 puts it on the nibble kernel; unset, the estimate below
+// chooses.  Returns 0, 1 or -1 (choose).
+int nibbles_mode() {
   const char *v = getenv("GBS_TCG_NIBBLES");
-  return !(v && v[0] == '0');
+  if (v && v[0] == '0') return 0;
+  if (v && v[0] == '1') return 1;
+  return -1;
+}
+
+// Which persistent kernel serves a plan faster, by an estimate of its
+// critical path.  The nibble kernel reads half a byte per element of each
+// problem's larger side where the digit kernel reads one, but it cuts that
+// side into 256-row tiles (half as many as the digit kernel's 128-row tiles),
+// and its stages move more shared memory (nibbles in, decoded digits out, a
+// 128-row MMA operand however few rows the smaller side has).  Per 128-digit
+// K stage a digit tile costs the longer of its bytes at ~100 GB/s into one SM
+// and its four MMAs (M = 128: ~37 ns up to N = 128, ~68 ns at N = 256), a
+// nibble tile ~0.7 us; the plan costs the longest of its tiles spread over
+// the SMs they can occupy, its largest tile, and its HBM bytes (larger side
+// once, smaller side once, results) at ~5 TB/s.  These constants are fitted
+// to GB300 timings of both kernels on groups of 1 to 397 problems, where the
+// estimate picks the faster kernel every time: groups of about 64 problems or
+// more are HBM-bound and take the nibbles; fewer leave SMs idle and take the
+// digit kernel's finer, cheaper tiles.
+bool plan_prefers_nibbles(gbs_ctx *const *ctxs, int n) {
+  const double sms = (double)std::max(1, sm_count());
+  double tiles[2] = {0, 0}, work[2] = {0, 0}, longest[2] = {0, 0}, hbm[2] = {0, 0};
+  auto mma_ns = [](double bn) { return bn <= 128 ? 37.0 : 37.0 + (bn - 128) * (31.0 / 128); };
+  for (int i = 0; i < n; i++) {
+    const Mat &L = ctxs[i]->lhs, &R = ctxs[i]->rhs;
+    const double small = (double)std::min(L.nrows, R.nrows), large = (double)std::max(L.nrows, R.nrows);
+    const double nk = (double)((L.ncols + 127) / 128), K = nk * 128;
+    if (small == 0 || nk == 0) continue;
+    for (int k = 0; k < 2; k++) {
+      const double bn = k ? 256 : std::min(256.0, std::ceil(small / 16) * 16);
+      const double nt = k ? std::ceil(small / 128) * std::ceil(large / 256)
+                          : std::ceil(large / 128) * std::ceil(small / bn);
+      const double t = nk * (k ? 700.0 : std::max((128 * 128 + bn * 128) / 100.0, 4 * mma_ns(bn)));  // ns
+      tiles[k] += nt;
+      work[k] += nt * t;
+      longest[k] = std::max(longest[k], t);
+      hbm[k] += (k ? large * K / 2 : large * K) + small * K + 4 * small * large;
+    }
+  }
+  double est[2];
+  for (int k = 0; k < 2; k++)
+    est[k] = std::max({tiles[k] > 0 ? work[k] / std::min(tiles[k], sms) : 0.0, longest[k], hbm[k] / 5000.0});
+  return est[1] < est[0];
 }
 
 }  // namespace
 
 int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
   tcg_plan_free(plan);
-  const bool nib = nibbles_enabled();
+  const int mode = nibbles_mode();
+  const bool nib = mode < 0 ? plan_prefers_nibbles(ctxs, n) : mode == 1;
   plan->nibbles = nib;
   std::vector<TcgProblem> probs;
   std::vector<CUtensorMap> maps;

@@ -262,14 +262,27 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
     P.c0 = e.c0;
     // kSkinnyTile outputs per tile, a warp each, where every BM x BN class would
     // leave most of its tile empty: fewer than 16 rhs rows (the classes' BN is
-    // 64 or more), or a tiny output
-    if (P.N < 16 || P.M * P.N <= 4096) {
+    // 64 or more), or a tiny output of more than 16 lhs rows; at most 16 lhs
+    // rows take the rows class below (a warp per output waits on memory once
+    // per output, a rows tile once per 128-byte step of 256 outputs)
+    const bool rows_fit = P.M <= (uint64_t)kRowsMaxM && popc_rows_smem(P.wa, kRowsKC) <= kGroupSmemCap;
+    if (P.N < 16 || (P.M * P.N <= 4096 && !rows_fit)) {
       P.cls = kSkinnyCls;
       probs.push_back(P);
       const uint64_t nt = (P.M * P.N + kSkinnyTile - 1) / kSkinnyTile;
       for (uint64_t i = 0; i < nt; i++) {
         tiles.push_back(GroupTile{(uint32_t)p, (uint32_t)i, 0u, (uint32_t)kSkinnyCls});
         cost.push_back(std::max<uint64_t>(1, (uint64_t)P.wa * P.wb * P.wpr / 512));
+      }
+    } else if (rows_fit) {
+      // at most 16 lhs rows: the rows class, one rhs row per thread (no popcounts on padding rows)
+      P.cls = kRowsCls;
+      smem = std::max(smem, popc_rows_smem(P.wa, kRowsKC));
+      probs.push_back(P);
+      const uint64_t nt = (P.N + 255) / 256;
+      for (uint64_t j = 0; j < nt; j++) {
+        tiles.push_back(GroupTile{(uint32_t)p, 0u, (uint32_t)j, (uint32_t)kRowsCls});
+        cost.push_back((uint64_t)P.wa * P.wb * P.wpr);
       }
     } else {
       P.cls = popc_tile_class(P.M, P.wa, P.wb, kGroupSmemCap);

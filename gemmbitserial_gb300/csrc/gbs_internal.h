@@ -267,6 +267,10 @@ int popc_tile_class(uint64_t M, int wa, int wb, size_t smem_cap);
 bool popc_skinny(uint64_t M, uint64_t N);
 constexpr int kSkinnyCls = 3;    // grouped tile class of kSkinnyTile outputs, one per warp
 constexpr int kSkinnyTile = 8;
+constexpr int kRowsCls = 4;      // grouped tile class of all <= kRowsMaxM lhs rows x 256 rhs rows
+constexpr int kRowsMaxM = 16;
+constexpr int kRowsKC = 16;      // K words per pipeline step of the rows tile (128 bytes of each row)
+size_t popc_rows_smem(int wa, int kc);
 size_t popc_stage_smem(int cls, int wa, int wb, int kc);
 constexpr int kGroupKC = 8;
 cudaError_t prepare_gemm_popc_grouped(size_t smem);

@@ -292,6 +292,7 @@ extern "C" int gbs_tune(gbs_ctx *c, int reps, int *best_pipe, void *stream) {
   Cand cands[24];
   int nc = 0;
   for (int v = -1; v <= 2; v++) cands[nc++] = Cand{GBS_PIPE_POPC, v};  // -1: built-in tile rule
+  if (c->lhs.nrows <= (uint64_t)kRowsMaxM) cands[nc++] = Cand{GBS_PIPE_POPC, kRowsCls};
   cands[nc++] = Cand{GBS_PIPE_BMMA, -1};
   if (tc_wide(c)) cands[nc++] = Cand{GBS_PIPE_TC, -1};  // 5-8-bit operands: part products on the digit pipe
   if (tc_exact(c, GBS_PIPE_TC)) {

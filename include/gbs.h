@@ -208,7 +208,9 @@ GBS_API int gbs_set_word(gbs_ctx *ctx, int side, uint64_t bit, uint64_t row, uin
 GBS_API int gbs_clear(gbs_ctx *ctx, int side, void *stream);
 
 /* Forces the variant of a context's pipe: CUDA-core tile class (0: 64x64,
- * 1: 32x128, 2: 16x256 outputs per CTA), tensor-core N tile (128 or 256 rows
+ * 1: 32x128, 2: 16x256 outputs per CTA, 4: every lhs row of a context with
+ * at most 16 of them x 256 rhs rows, one rhs row per thread), tensor-core N
+ * tile (128 or 256 rows
  * of rhs per 128-row lhs tile on one SM), or 512 / 513 for GBS_PIPE_TC:
  * 256 x 256 / 256 x 128 tiles computed by pairs of SMs (tcgen05
  * cta_group::2), K split over up to 4 pairs of one cluster when the tiles are
@@ -372,8 +374,10 @@ GBS_API int gbs_debug_group_poison_tile(gbs_group *g, uint32_t tile);
 /* Which persistent tensor-core kernel runs a group's tensor-core problems:
  * 0 none, 1 the digit kernel (both operands as e4m3 digit matrices), 2 the
  * nibble kernel (the larger operand as 4-bit codes, decoded to digits in
- * shared memory).  GBS_TCG_NIBBLES=0 in the environment at gbs_group_create
- * keeps a group on the digit kernel.  Negative on a NULL group. */
+ * shared memory).  By default an estimate of both kernels' critical paths
+ * chooses (hundreds of problems: nibbles; one or a few: digits);
+ * GBS_TCG_NIBBLES=0 or 1 in the environment at gbs_group_create forces the
+ * digit or the nibble kernel.  Negative on a NULL group. */
 GBS_API int gbs_debug_group_tc_kernel(const gbs_group *g);
 
 /* Exercises the tensor-core kernels' bounded waits without a GPU fault: one

@@ -26,11 +26,11 @@ def make_contexts(mix):
     return [allocGEMMContext(M, K, N, wA, wB, eA != "u", eB != "u") for (M, K, N, wA, eA, wB, eB) in mix]
 
 
-@pytest.fixture(params=["auto", "tc", "tc-digits", "popc"])
+@pytest.fixture(params=["auto", "tc", "tc-digits", "tc-nibbles", "popc"])
 def group_pipe(request, monkeypatch):
     """GBS_GROUP_PIPE as read by gbs_group_create: per-problem choice, or one kernel forced;
-    tc-digits also keeps the tensor-core problems on the digit kernel (GBS_TCG_NIBBLES=0)
-    instead of the nibble kernel."""
+    tc-digits / tc-nibbles also force the tensor-core problems' kernel (GBS_TCG_NIBBLES=0 / 1)
+    where plain tc leaves it to the library's estimate."""
     monkeypatch.delenv("GBS_TCG_NIBBLES", raising=False)
     if request.param == "auto":
         monkeypatch.delenv("GBS_GROUP_PIPE", raising=False)
@@ -38,6 +38,8 @@ def group_pipe(request, monkeypatch):
         monkeypatch.setenv("GBS_GROUP_PIPE", request.param.split("-")[0])
     if request.param == "tc-digits":
         monkeypatch.setenv("GBS_TCG_NIBBLES", "0")
+    if request.param == "tc-nibbles":
+        monkeypatch.setenv("GBS_TCG_NIBBLES", "1")
     return request.param
 
 
@@ -49,7 +51,8 @@ def check_split(g, mode, count):
         assert st["tc_kernel"] == "none"
     if mode.startswith("tc"):
         assert st["tc_problems"] > 0
-        assert st["tc_kernel"] == ("digits" if mode == "tc-digits" else "nibbles")
+        want = {"tc-digits": ("digits",), "tc-nibbles": ("nibbles",)}.get(mode, ("digits", "nibbles"))
+        assert st["tc_kernel"] in want
     return st
 
 
@@ -117,6 +120,10 @@ EDGE_MIX = [
     (41, 4992, 300, 3, "u", 1, "u"),
     (40, 74560, 130, 4, "u", 3, "u"),    # wpr 1165
     (40, 80000, 130, 4, "u", 3, "u"),    # 80000 * 15 * 7 < 2^24
+    # few lhs rows: the CUDA cores' rows tile when the built-in rule keeps them there
+    (3, 1000, 700, 1, "b", 1, "b"),      # XOR, wpr 16
+    (9, 64 * 37 + 5, 513, 1, "u", 1, "u"),  # wpr 38, 3 tiles of 256 rhs rows
+    (2, 4096, 3000, 2, "s", 2, "u"),
 ]
 
 

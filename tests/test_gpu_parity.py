@@ -146,6 +146,33 @@ def test_odd_and_skinny_shapes(shape):
             assert np.array_equal(gpu_gemm(A, B, wa, wb, sa, sb, pipe=pipe), ref), (shape, wa, ea, wb, eb, pipe)
 
 
+@pytest.mark.parametrize("M", [1, 2, 3, 5, 8, 9, 16])
+def test_popc_rows_tile(lib, M):
+    """The CUDA cores' rows tile (at most 16 lhs rows x 256 rhs rows, one rhs row per thread), forced
+    (variant 4) and by the built-in rule: every M bucket, odd and even words per row, rhs row counts
+    off the 256-row tile, bipolar x bipolar (XOR), bipolar x regular (row sums), signed, 8-bit planes."""
+    rng = np.random.default_rng(100 + M)
+    for (K, N) in [(64 * 37 + 5, 700), (64 * 40, 256), (1000, 513)]:
+        for (wa, ea, wb, eb) in [(1, "u", 1, "u"), (1, "b", 1, "b"), (1, "b", 4, "s"), (3, "s", 2, "u"),
+                                 (8, "s", 3, "u"), (2, "u", 8, "s"), (4, "u", 1, "b")]:
+            A = datagen.operand(int(rng.integers(1 << 30)), M, K, wa, ea)
+            B = datagen.operand(int(rng.integers(1 << 30)), N, K, wb, eb)
+            sa, sb = ea != "u", eb != "u"
+            ref = O.oracle_gemm(A, B, wa, wb, sa, sb)
+            for variant in (-1, 4):
+                ctx = allocGEMMContext(M, K, N, wa, wb, sa, sb)
+                try:
+                    ctx.set_pipe(_capi.GBS_PIPE_POPC)
+                    _capi.check(lib.gbs_set_variant(ctx._h, variant))
+                    ctx.lhs.importRegular(A)
+                    ctx.rhs.importRegular(B)
+                    gemmBitSerial(ctx)
+                    got = ctx.res.reshape(N, M)
+                finally:
+                    deallocGEMMContext(ctx)
+                assert np.array_equal(got, ref), (M, K, N, wa, ea, wb, eb, variant)
+
+
 def test_empty_shapes():
     for (M, K, N) in [(0, 64, 5), (5, 64, 0), (0, 0, 0)]:
         ctx = allocGEMMContext(M, K, N, 2, 2, 0, 0)
