@@ -180,23 +180,28 @@ __device__ __forceinline__ void popc_tile(const TileArgs &g, uint64_t m0, uint64
   }
 }
 
-// The rows tile: every lhs row of a problem with at most MB (<= 16) of them x
-// NT rhs rows.  Thread t owns rhs row n0 + t and its M outputs, so popcounts
-// are spent on at most the next power of two of M lhs rows instead of a
-// 16- or 32-row tile's padding (for M = 1 the BM x BN classes do 16x the
-// work).  The pipeline steps over (rhs plane j, K chunk) pairs: a stage holds
-// one K chunk of rhs plane j for the NT rows and of every lhs plane for the
-// 16 staged lhs rows, so its shared memory does not grow with wb.  The lhs
-// words are read as broadcasts.  Ends with a __syncthreads().
+// The rows tile: every lhs row of a problem with at most 16 of them x
+// rows_tile_n(M) rhs rows.  TPR threads share one rhs row, each taking MT of
+// the lhs rows (MT * TPR = M rounded up to a power of two), so popcounts are
+// spent on at most that many lhs rows instead of a 16- or 32-row tile's
+// padding (for M = 1 the BM x BN classes do 16x the work), and no thread
+// counts more than 4 lhs rows per word (past that a tile's popcounts, not its
+// loads, set its time).  The pipeline steps over (rhs plane j, K chunk) pairs:
+// a stage holds one K chunk of rhs plane j for the tile's rhs rows and of
+// every lhs plane for the 16 staged lhs rows, so its shared memory does not
+// grow with wb.  The lhs words are read as broadcasts, an rhs word by its TPR
+// threads at once.  Ends with a __syncthreads().
 constexpr int kRowsStagedRows = kRowsMaxM;
 __host__ __device__ constexpr size_t rows_stage_words(int wa, int kc) {
   return (size_t)(wa * kRowsStagedRows + NT) * (kc + 2);
 }
 
-template <int MB, int KC, bool XOR>
+template <int MT, int TPR, int KC, bool XOR>
 __device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, uint64_t *smem) {
   constexpr int LDW = KC + 2;
+  constexpr int BNR = NT / TPR;  // rhs rows of the tile
   const int wa = g.wa, wb = g.wb, tid = threadIdx.x;
+  const int r = tid / TPR, q = tid % TPR;  // the thread's rhs row and lhs rows q*MT .. q*MT + MT-1
   const int stage_words = (int)rows_stage_words(wa, KC);
   const uint64_t wpr = g.wpr;
   const int nchunks = (int)((wpr + KC - 1) / KC);
@@ -208,7 +213,7 @@ __device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, u
     uint64_t *s = smem + st * stage_words;
     const int a_rows = wa * kRowsStagedRows;
     const int piece = (wpr & 1) ? 1 : 2;  // odd word counts (64-bit column padding): 8-byte pieces
-    const int per_row = KC / piece, all = (a_rows + NT) * per_row;
+    const int per_row = KC / piece, all = (a_rows + BNR) * per_row;
     for (int idx = tid; idx < all; idx += NT) {
       const int row = idx / per_row, p = idx % per_row;
       const bool isA = row < a_rows;
@@ -217,9 +222,9 @@ __device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, u
       uint64_t grow;
       bool ok;
       if (isA) {
-        const int plane = row / kRowsStagedRows, r = row % kRowsStagedRows;
+        const int plane = row / kRowsStagedRows, rr = row % kRowsStagedRows;
         base = g.A + plane * g.a_plane;
-        grow = (uint64_t)r;
+        grow = (uint64_t)rr;
         ok = k < wpr && grow < g.a_rows;
       } else {
         base = g.B + j * g.b_plane;
@@ -232,9 +237,9 @@ __device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, u
     }
   };
 
-  uint32_t acc[MB];
+  uint32_t acc[MT];
 #pragma unroll
-  for (int m = 0; m < MB; m++) acc[m] = 0u;
+  for (int m = 0; m < MT; m++) acc[m] = 0u;
 
   if (nsteps > 0) {
     load_stage(0, 0);
@@ -251,45 +256,47 @@ __device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, u
     __syncthreads();
     const int j = st / nchunks;
     const uint64_t *sa = smem + (st & 1) * stage_words;
-    const uint64_t *pb = sa + (wa * kRowsStagedRows + tid) * LDW;
+    const uint64_t *pb = sa + (wa * kRowsStagedRows + r) * LDW;
 #pragma unroll 1
     for (int i = 0; i < wa; i++) {
-      const uint64_t *pa = sa + i * kRowsStagedRows * LDW;
+      const uint64_t *pa = sa + (i * kRowsStagedRows + q * MT) * LDW;
       const uint32_t al = alpha_of(i, j, g.neg_i, g.neg_j, g.shift, XOR);  // weights fold in per count (mod 2^32)
-      constexpr int kUnroll = MB >= 8 ? 1 : 8 / MB;  // about 8 independent counts per unrolled step
+      constexpr int kUnroll = 8 / MT;  // about 8 independent counts per unrolled step
 #pragma unroll kUnroll
       for (int kp = 0; kp < KC / 2; kp++) {
         const ulonglong2 b = *reinterpret_cast<const ulonglong2 *>(pb + 2 * kp);
 #pragma unroll
-        for (int m = 0; m < MB; m++)
+        for (int m = 0; m < MT; m++)
           acc[m] += pc2<XOR>(*reinterpret_cast<const ulonglong2 *>(pa + m * LDW + 2 * kp), b) * al;
       }
     }
     __syncthreads();
   }
 
-  const uint64_t gn = n0 + tid;
+  const uint64_t gn = n0 + (uint64_t)r;
   if (gn < g.N) {
     const uint32_t bn = g.c0 - (g.rb ? (uint32_t)g.rb[gn] : 0u);
 #pragma unroll
-    for (int m = 0; m < MB; m++)
-      if (m < (int)g.M) g.C[gn * g.M + m] = (int32_t)(acc[m] + bn - (g.ra ? (uint32_t)g.ra[m] : 0u));
+    for (int mm = 0; mm < MT; mm++) {
+      const int m = q * MT + mm;
+      if (m < (int)g.M) g.C[gn * g.M + m] = (int32_t)(acc[mm] + bn - (g.ra ? (uint32_t)g.ra[m] : 0u));
+    }
   }
 }
 
 template <int KC, bool XOR>
 __device__ __forceinline__ void popc_rows_dispatch(const TileArgs &g, uint64_t n0, uint64_t *smem) {
-  if (g.M <= 1) popc_rows_tile<1, KC, XOR>(g, n0, smem);
-  else if (g.M <= 2) popc_rows_tile<2, KC, XOR>(g, n0, smem);
-  else if (g.M <= 4) popc_rows_tile<4, KC, XOR>(g, n0, smem);
-  else if (g.M <= 8) popc_rows_tile<8, KC, XOR>(g, n0, smem);
-  else popc_rows_tile<16, KC, XOR>(g, n0, smem);
+  if (g.M <= 1) popc_rows_tile<1, 1, KC, XOR>(g, n0, smem);
+  else if (g.M <= 2) popc_rows_tile<2, 1, KC, XOR>(g, n0, smem);
+  else if (g.M <= 4) popc_rows_tile<4, 1, KC, XOR>(g, n0, smem);
+  else if (g.M <= 8) popc_rows_tile<4, 2, KC, XOR>(g, n0, smem);
+  else popc_rows_tile<4, 4, KC, XOR>(g, n0, smem);
 }
 
 template <bool XOR>
 __global__ void __launch_bounds__(NT, 2) gemm_popc_rows(TileArgs g) {
   extern __shared__ __align__(16) uint64_t smem[];
-  popc_rows_dispatch<kRowsKC, XOR>(g, (uint64_t)blockIdx.x * NT, smem);
+  popc_rows_dispatch<kRowsKC, XOR>(g, (uint64_t)blockIdx.x * rows_tile_n(g.M), smem);
 }
 
 template <int BM, int BN, int KC, bool XOR>
@@ -394,7 +401,7 @@ __global__ void __launch_bounds__(NT, 2) gemm_popc_grouped(const GroupProblem *_
       continue;
     }
     const bool rows = tl.cls == kRowsCls;
-    const int bm = rows ? kRowsMaxM : tile_bm((int)tl.cls), bn = rows ? NT : tile_bn((int)tl.cls);
+    const int bm = rows ? kRowsMaxM : tile_bm((int)tl.cls), bn = rows ? rows_tile_n(P.M) : tile_bn((int)tl.cls);
     const uint64_t m0 = (uint64_t)tl.mt * bm, n0 = (uint64_t)tl.nt * bn;
     if (m0 >= P.M || n0 >= P.N || P.wa < 1 || P.wa > kMaxBits || P.wb < 1 || P.wb > kMaxBits ||
         (rows && P.M > (uint64_t)kRowsMaxM)) {
@@ -470,7 +477,8 @@ cudaError_t run_rows(const TileArgs &t, cudaStream_t s) {
   auto kern = gemm_popc_rows<XOR>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  kern<<<(unsigned)((t.N + NT - 1) / NT), NT, smem, s>>>(t);
+  const uint64_t bnr = rows_tile_n(t.M);
+  kern<<<(unsigned)((t.N + bnr - 1) / bnr), NT, smem, s>>>(t);
   count_launch();
   return cudaGetLastError();
 }

@@ -537,7 +537,11 @@ int tcg_plan_build(TcgPlan *plan, gbs_ctx *const *ctxs, int n) {
       P.idesc = (1u << 4) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
       P.w4 = MB.nbits > 3 ? 1u : 0u;
       tc_digit_table(MB, P.tab);
-      if (!tc_map_u8(&m2[0], c->digits[sa], MA.dcols, MA.drows, 128) ||
+      // a smaller side of at most 128 rows loads only its rows (16-row blocks) into the
+      // 128-row MMA-A slot: the slot's other rows feed accumulator lanes no store reads
+      const uint32_t a_box = MA.nrows <= 128 ? (uint32_t)std::max<uint64_t>(16, (MA.nrows + 15) / 16 * 16) : 128u;
+      P.a_bytes = a_box * 128u;
+      if (!tc_map_u8(&m2[0], c->digits[sa], MA.dcols, MA.drows, a_box) ||
           !tc_map_nibbles(&m2[1], c->nibbles[sb], MB.dcols, MB.drows))
         return fail(GBS_EUNSUPPORTED, "tensor-core plan: tensor map encoding failed");
       rt = (uint32_t)((MA.nrows + 127) / 128);

@@ -28,7 +28,7 @@
 //
 // Warps: 0 nibble loads (lane 0); 1 TMEM allocation and MMA issue (lane 0);
 // 2 MMA-A digit loads (lane 0); 3-6 epilogue of tile j while the MMAs of tile
-// j + 1 run; 7-14 decoders, one row of the 256-row stage per thread.  Every
+// j + 1 run; 7-22 decoders, half a row of the 256-row stage per thread.  Every
 // mbarrier wait is bounded; on timeout the CTA sets a bit in the caller's
 // error word, stops issuing, drains what it issued and frees TMEM.
 #include <algorithm>
@@ -39,7 +39,7 @@
 namespace gbs {
 namespace {
 
-constexpr int kNbDecWarps = 8;  // 256 decoder threads: one row of the 256-row MMA-B stage each
+constexpr int kNbDecWarps = 16;  // 512 decoder threads: half a row (64 codes) of the 256-row MMA-B stage each
 constexpr int kNbDec0 = 7;      // first decoder warp
 constexpr int kNbThreads = 32 * (kNbDec0 + kNbDecWarps);
 constexpr int kNbASlots = 4;  // MMA-A digit stages, 128 rows x 128 digits
@@ -59,7 +59,8 @@ __device__ __forceinline__ uint32_t snake(uint32_t j, uint32_t b, uint32_t G) {
 }
 
 __device__ __forceinline__ bool ntile_ok(const TcgTile &t, const TcgProblem &P, uint32_t nprob) {
-  return t.p < nprob && P.nk > 0 && (t.r + 1) * 128u <= P.a_rows && (t.c + 1) * 256u <= P.b_rows;
+  return t.p < nprob && P.nk > 0 && (t.r + 1) * 128u <= P.a_rows && (t.c + 1) * 256u <= P.b_rows &&
+         P.a_bytes >= 2048u && P.a_bytes <= kNbASlotBytes && P.a_bytes % 2048u == 0;
 }
 
 // prmt.b32 in its generic mode: result byte i is source byte s[4i+2:4i] of
@@ -82,13 +83,15 @@ __device__ __forceinline__ uint32_t lut4(uint32_t x, const uint32_t (&tab)[4]) {
   return (lo & ~m) | (hi & m);
 }
 
-// One row of the MMA-B stage: 64 bytes of codes (16-byte chunks 64-byte
-// swizzled) -> 128 e4m3 bytes (16-byte chunks 128-byte swizzled, the MMA's
-// K-major layout).
+// Half `half` of one row of the MMA-B stage: 32 of its 64 bytes of codes
+// (16-byte chunks 64-byte swizzled) -> 64 of its 128 e4m3 bytes (16-byte
+// chunks 128-byte swizzled, the MMA's K-major layout).
 template <bool W4>
-__device__ __forceinline__ void decode_row(const uint8_t *src, uint8_t *dst, uint32_t row, const uint32_t (&tab)[4]) {
+__device__ __forceinline__ void decode_half_row(const uint8_t *src, uint8_t *dst, uint32_t row, uint32_t half,
+                                                const uint32_t (&tab)[4]) {
 #pragma unroll
-  for (uint32_t j = 0; j < 4; j++) {  // codes of columns 32j .. 32j + 31
+  for (uint32_t jj = 0; jj < 2; jj++) {  // codes of columns 32j .. 32j + 31
+    const uint32_t j = 2 * half + jj;
     const uint4 v = *reinterpret_cast<const uint4 *>(src + ((j ^ ((row >> 1) & 3u)) << 4));
     const uint4 d0 = make_uint4(lut4<W4>(v.x, tab), lut4<W4>(v.x >> 16, tab), lut4<W4>(v.y, tab),
                                 lut4<W4>(v.y >> 16, tab));
@@ -97,6 +100,25 @@ __device__ __forceinline__ void decode_row(const uint8_t *src, uint8_t *dst, uin
     *reinterpret_cast<uint4 *>(dst + (((2 * j) ^ (row & 7u)) << 4)) = d0;
     *reinterpret_cast<uint4 *>(dst + (((2 * j + 1) ^ (row & 7u)) << 4)) = d1;
   }
+}
+
+// 16 accumulator columns of the warp's 32 TMEM lanes, without the wait.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+}
+// Marks registers filled by TMEM loads as produced after the tcgen05.wait::ld
+// issued just before (volatile asm keeps its place in program order), so no
+// use of them is scheduled ahead of the wait.
+__device__ __forceinline__ void regs_after_wait(uint32_t (&v)[16]) {
+  asm volatile(""
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                 "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15])
+               :
+               : "memory");
 }
 
 // Rows [row, row + 256) x codes [128 k, 128 k + 128) of a nibble matrix: the
@@ -166,7 +188,6 @@ __global__ void __launch_bounds__(kNbThreads, 1)
       const bool nib = warp == 0;
       const int slots = nib ? kNbNSlots : kNbASlots;
       const uint32_t full = nib ? n_full : a_full, empty = nib ? n_empty : a_empty;
-      const uint32_t bytes = nib ? kNbNSlotBytes : kNbASlotBytes;
       uint8_t *ring = nib ? nring : aring;
       uint32_t it = 0;
       bool stop = false;
@@ -178,6 +199,7 @@ __global__ void __launch_bounds__(kNbThreads, 1)
         const TcgProblem P = probs[tl.p];
         if (!ntile_ok(tl, P, nprob)) continue;
         const CUtensorMap *m = maps + 2 * tl.p + (nib ? 1 : 0);
+        const uint32_t bytes = nib ? kNbNSlotBytes : P.a_bytes;
         asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m) : "memory");
         for (uint32_t k = 0; k < P.nk; k++, it++) {
           const uint32_t s = it % slots, use = it / slots;
@@ -186,7 +208,7 @@ __global__ void __launch_bounds__(kNbThreads, 1)
             break;
           }
           mbar_expect_tx(full + 8 * s, bytes);
-          const uint32_t dst = smem_u32(ring + s * bytes);
+          const uint32_t dst = smem_u32(ring + s * (nib ? kNbNSlotBytes : kNbASlotBytes));
           if (nib) tma_load_nibbles(dst, m, (int)k, tl.c * 256u, full + 8 * s);
           else tma_load_digits(dst, m, (int)k, tl.r * 128u, full + 8 * s);
         }
@@ -260,31 +282,40 @@ __global__ void __launch_bounds__(kNbThreads, 1)
       const uint32_t taddr = tmem + acc * kNbAccCols + ((uint32_t)(q * 32) << 16);
       const uint32_t nb = P.swap ? P.M : P.N;  // rows of MMA-B (the tile's columns)
       const uint32_t ncols = min(256u, nb - min(nb, tl.c * 256u));
+      // a warp whose 32 accumulator rows all lie past the smaller side's rows stores nothing:
+      // it skips the TMEM loads too (in a group most smaller sides have a few dozen rows)
+      const uint32_t arows = P.swap ? P.N : P.M;
+      const bool live = tl.r * 128u + (uint32_t)(q * 32) < arows;
 #pragma unroll 1
-      for (uint32_t col = 0; col < ncols; col += 16) {
-        uint32_t v[16];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-            : "r"(taddr + col));
+      for (uint32_t col = 0; live && col < ncols; col += 32) {
+        // two 16-column loads behind one wait (columns up to col + 31 < 256 stay inside the
+        // accumulator; only the stores are bounded by ncols)
+        uint32_t v[2][16];
+#pragma unroll
+        for (int h = 0; h < 2; h++) tmem_ld16(taddr + col + 16 * h, v[h]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        int32_t o[16];
 #pragma unroll
-        for (int i = 0; i < 16; i++) o[i] = __float2int_rn(__uint_as_float(v[i]));
-        const uint32_t c0 = tl.c * 256u + col;
-        if (!P.swap) {  // row = m, column = n: lanes write 32 consecutive m of one n
-          store_result_cols<16>(P.C, P.M, P.N, row, c0, o);
-        } else if (row < P.N) {  // row = n, column = m: each lane writes a run of its result row
-          int32_t *dst = P.C + (uint64_t)row * P.M + c0;
-          if ((P.M & 3u) == 0) {
+        for (int h = 0; h < 2; h++) regs_after_wait(v[h]);
 #pragma unroll
-            for (int i = 0; i < 16; i += 4)
-              if (c0 + i < P.M) *reinterpret_cast<int4 *>(dst + i) = make_int4(o[i], o[i + 1], o[i + 2], o[i + 3]);
-          } else {
+        for (int h = 0; h < 2; h++) {
+          const uint32_t c0 = tl.c * 256u + col + 16u * h;
+          if (col + 16u * h >= ncols) break;
+          int32_t o[16];
 #pragma unroll
-            for (int i = 0; i < 16; i++)
-              if (c0 + i < P.M) dst[i] = o[i];
+          for (int i = 0; i < 16; i++) o[i] = __float2int_rn(__uint_as_float(v[h][i]));
+          if (!P.swap) {  // row = m, column = n: lanes write 32 consecutive m of one n
+            store_result_cols<16>(P.C, P.M, P.N, row, c0, o);
+          } else if (row < P.N) {  // row = n, column = m: each lane writes a run of its result row
+            int32_t *dst = P.C + (uint64_t)row * P.M + c0;
+            if ((P.M & 3u) == 0) {
+#pragma unroll
+              for (int i = 0; i < 16; i += 4)
+                if (c0 + i < P.M) *reinterpret_cast<int4 *>(dst + i) = make_int4(o[i], o[i + 1], o[i + 2], o[i + 3]);
+            } else {
+#pragma unroll
+              for (int i = 0; i < 16; i++)
+                if (c0 + i < P.M) dst[i] = o[i];
+            }
           }
         }
       }
@@ -295,7 +326,7 @@ __global__ void __launch_bounds__(kNbThreads, 1)
     }
   } else {
     // ---------------- decoders: thread -> row `row` of every 256-row MMA-B stage
-    const uint32_t row = (uint32_t)(tid - 32 * kNbDec0);
+    const uint32_t row = (uint32_t)(tid - 32 * kNbDec0) & 255u, half = (uint32_t)(tid - 32 * kNbDec0) >> 8;
     uint32_t it = 0;
     bool ok = true;
     for (uint32_t j = 0; ok; j++) {
@@ -317,8 +348,8 @@ __global__ void __launch_bounds__(kNbThreads, 1)
         }
         const uint8_t *src = nring + ns * kNbNSlotBytes + row * 64u;
         uint8_t *dst = bring + bs * kNbBSlotBytes + row * 128u;
-        if (P.w4) decode_row<true>(src, dst, row, tab);
-        else decode_row<false>(src, dst, row, tab);
+        if (P.w4) decode_half_row<true>(src, dst, row, half, tab);
+        else decode_half_row<false>(src, dst, row, half, tab);
         // generic-proxy writes become visible to tcgen05.mma (async proxy): each thread's
         // proxy fence, the warp's barrier, then one mbarrier arrival (release) per warp
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

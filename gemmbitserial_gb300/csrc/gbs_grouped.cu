@@ -279,7 +279,7 @@ int gbs_group_create(gbs_ctx *const *ctxs, int count, gbs_group **out) {
       P.cls = kRowsCls;
       smem = std::max(smem, popc_rows_smem(P.wa, kRowsKC));
       probs.push_back(P);
-      const uint64_t nt = (P.N + 255) / 256;
+      const uint64_t bnr = (uint64_t)rows_tile_n(P.M), nt = (P.N + bnr - 1) / bnr;
       for (uint64_t j = 0; j < nt; j++) {
         tiles.push_back(GroupTile{(uint32_t)p, 0u, (uint32_t)j, (uint32_t)kRowsCls});
         cost.push_back((uint64_t)P.wa * P.wb * P.wpr);

@@ -127,6 +127,8 @@ struct TcgProblem {
   uint32_t swap;            // 1: MMA-A = rhs (tile rows are n), MMA-B = lhs (columns are m)
   uint32_t w4;              // nibble kernel: MMA-B codes of 4 bits (the two-table lookup)
   uint32_t tab[4];          // nibble kernel: e4m3 byte of every MMA-B code
+  uint32_t a_bytes;         // nibble kernel: MMA-A bytes loaded per stage (rows of the smaller side, 16-row
+                            // multiples up to 128, x 128 digits; the tile's other rows only feed unstored lanes)
 };
 
 // One output tile: problem, 128-row block of MMA-A, bn-column block of MMA-B.
@@ -270,6 +272,8 @@ constexpr int kSkinnyTile = 8;
 constexpr int kRowsCls = 4;      // grouped tile class of all <= kRowsMaxM lhs rows x 256 rhs rows
 constexpr int kRowsMaxM = 16;
 constexpr int kRowsKC = 16;      // K words per pipeline step of the rows tile (128 bytes of each row)
+// rhs rows of a rows tile for M lhs rows: 256 threads, 1, 2 or 4 of them per rhs row
+__host__ __device__ inline int rows_tile_n(uint64_t M) { return M <= 4 ? 256 : (M <= 8 ? 128 : 64); }
 size_t popc_rows_smem(int wa, int kc);
 size_t popc_stage_smem(int cls, int wa, int wb, int kc);
 constexpr int kGroupKC = 8;
