@@ -14,6 +14,7 @@ GBS_OK, GBS_EINVAL, GBS_ENOMEM, GBS_ECUDA, GBS_ESTATE, GBS_ETIMEOUT, GBS_EUNSUPP
 GBS_I8, GBS_U8, GBS_I16, GBS_I32, GBS_F32 = range(5)
 GBS_LHS, GBS_RHS = 0, 1
 GBS_PIPE_AUTO, GBS_PIPE_POPC, GBS_PIPE_BMMA, GBS_PIPE_TC, GBS_PIPE_TC_PAIRS, GBS_PIPE_TC_SMEM = 0, 1, 2, 3, 4, 5
+GBS_HOST_IMPORT_AUTO, GBS_HOST_IMPORT_STAGED = 0, 1
 
 # Every entry point include/gbs.h declares, with (restype, argtypes).
 u64, i32, vp = C.c_uint64, C.c_int, C.c_void_p
@@ -50,6 +51,7 @@ SIGNATURES = {
     "gbs_export": (i32, [vp, i32, vp, vp]),
     "gbs_get_planes": (i32, [vp, i32, vp, vp]),
     "gbs_set_pipe": (i32, [vp, i32]),
+    "gbs_set_host_import": (i32, [vp, i32]),
     "gbs_set_variant": (i32, [vp, i32]),
     "gbs_gemm_noalloc": (i32, [vp, i32, vp, i32, u64, u64, u64, u64, u64, i32, i32, vp, vp]),
     "gbs_noalloc_scratch_bytes": (u64, []),

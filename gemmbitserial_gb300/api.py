@@ -224,6 +224,12 @@ class GEMMContext:
     def set_pipe(self, pipe: int) -> None:
         _capi.check(_capi.load().gbs_set_pipe(self._h, pipe))
 
+    def set_host_import(self, mode: int) -> None:
+        """GBS_HOST_IMPORT_AUTO (read host sources in place where the device can) or
+        GBS_HOST_IMPORT_STAGED (copy-engine copies; for contexts whose imports run beside
+        another context's GEMM)."""
+        _capi.check(_capi.load().gbs_set_host_import(self._h, mode))
+
     @property
     def pipe(self) -> int:
         return self._info().pipe

@@ -462,7 +462,9 @@ int gbs_import(gbs_ctx *c, int side, const void *src, int dtype, int col_major, 
     }
   }
   cudaError_t e = cudaSuccess;
-  const void *view = (n && !is_device_ptr(src)) ? device_view(src, c->device, true) : nullptr;
+  const void *view = (n && !is_device_ptr(src) && c->host_import != GBS_HOST_IMPORT_STAGED)
+                         ? device_view(src, c->device, true)
+                         : nullptr;
   if (view) {  // host memory the device reads directly: the pack kernel is the copy
     if (!col_major) {
       e = launch_pack_rows(m, view, dtype, 0, m.nrows_a, digits, dtab, s);
@@ -717,6 +719,14 @@ int gbs_set_variant(gbs_ctx *c, int variant) {
     return fail(GBS_EINVAL,
                 "gbs_set_variant: variant must be -1, 0..2, 4, 128, 256, 512..515, 1281, 1282, 1284, 2561, 2562 or 2564");
   c->variant = variant;
+  return GBS_OK;
+}
+
+int gbs_set_host_import(gbs_ctx *c, int mode) {
+  if (!c) return fail(GBS_EINVAL, "gbs_set_host_import: ctx is NULL");
+  if (mode != GBS_HOST_IMPORT_AUTO && mode != GBS_HOST_IMPORT_STAGED)
+    return fail(GBS_EINVAL, "gbs_set_host_import: mode must be GBS_HOST_IMPORT_AUTO or GBS_HOST_IMPORT_STAGED");
+  c->host_import = mode;
   return GBS_OK;
 }
 

@@ -214,6 +214,7 @@ struct gbs_ctx {
   // larger operand's form for the nibble kernel, built like the digits
   uint8_t *nibbles[2] = {nullptr, nullptr};
   bool nibbles_valid[2] = {false, false};
+  int host_import = 0;  // GBS_HOST_IMPORT_*: how gbs_import reads host-memory sources
   alignas(64) unsigned char tc_map_da[128];
   alignas(64) unsigned char tc_map_db[128];
   bool digit_maps_ready = false;

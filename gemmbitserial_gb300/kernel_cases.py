@@ -12,6 +12,8 @@ prints "ok <case>".  The kernels each case launches:
   gemm_bmma       the same on b1 mma.sync (gemm_bmma_kernel)
   gemm_tc_smem    the same, planes decoded in shared memory (gemm_tc_kernel)
   gemm_skinny     8x8192x8 u1 x u1 (gemm_popc_skinny)
+  gemm_rows       9 x 8192 x 32768, 1-bit unsigned x 2-bit signed on the CUDA cores (gemm_popc_rows: at most
+                  16 lhs rows, 64 rhs rows x every lhs row per CTA)
   import_device   importRegular of the 2048x4096 int8 lhs from device memory, planes + digits (pack_rowmajor)
   import_host     the same from pinned host memory, read over the host link (pack_rowmajor)
   import_colmajor the same operand read column-major (pack_colmajor)
@@ -30,7 +32,7 @@ import ctypes as C
 import os
 import sys
 
-CASES = ["gemm", "gemm_streamk", "gemm_popc", "gemm_bmma", "gemm_tc_smem", "gemm_skinny", "import_device",
+CASES = ["gemm", "gemm_streamk", "gemm_popc", "gemm_bmma", "gemm_tc_smem", "gemm_skinny", "gemm_rows", "import_device",
          "import_host", "import_colmajor", "import_quantize", "expand", "group", "group_small", "adjoint",
          "adjoint_simt"]
 
@@ -74,7 +76,13 @@ def main() -> None:
             pipe, variant = _capi.GBS_PIPE_TC_SMEM, 256
         elif case == "gemm_skinny":
             name = "gemm_8x8192x8_u1u1"
-        c, dA, dB = ctx_of(name, pipe, variant)
+        if case == "gemm_rows":
+            c = allocGEMMContext(9, 8192, 32768, 1, 2, False, True)
+            c.set_pipe(_capi.GBS_PIPE_POPC)
+            dA = torch.from_numpy(datagen.operand(datagen.SEED_BASE + 61, 9, 8192, 1, "u")).to(dev)
+            dB = torch.from_numpy(datagen.operand(datagen.SEED_BASE + 62, 32768, 8192, 2, "s")).to(dev)
+        else:
+            c, dA, dB = ctx_of(name, pipe, variant)
         with torch.cuda.stream(s):
             c.lhs.importRegular(dA, stream=s)
             c.rhs.importRegular(dB, stream=s)

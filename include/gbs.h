@@ -228,6 +228,23 @@ GBS_API int gbs_set_variant(gbs_ctx *ctx, int variant);
 /* Forces the pipe of a context's forward GEMM (GBS_PIPE_*). */
 GBS_API int gbs_set_pipe(gbs_ctx *ctx, int pipe);
 
+/* How gbs_import brings a host-memory source of this context to the GPU. */
+enum {
+  GBS_HOST_IMPORT_AUTO = 0,  /* the pack kernel reads the source in place where the device can
+                                (pinned memory; pageable memory where the GPU walks the host page
+                                tables), unless GBS_HOST_DIRECT=0; otherwise staged copies */
+  GBS_HOST_IMPORT_STAGED = 1 /* copy-engine copies into a device buffer, in chunks whose packing
+                                overlaps the next copy */
+};
+/* Sets a context's host import mode (GBS_HOST_IMPORT_*; default AUTO).  Reading
+ * in place needs no copy and is the faster choice while the GPU runs one
+ * context at a time; staged copies leave the transfer to the copy engines and
+ * the SMs to other work, the faster choice when another context's GEMM holds
+ * most SMs at the same time (two host threads driving two contexts).  Either
+ * way gbs_import returns once the source has been read.  No reference
+ * counterpart. */
+GBS_API int gbs_set_host_import(gbs_ctx *ctx, int mode);
+
 /* ---- one-shot GEMM without allocation ---------------------------------- *
  * No counterpart in the reference.  For callers that cannot let the library
  * call cudaMalloc -- code running while a stream is captured into a CUDA

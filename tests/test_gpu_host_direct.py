@@ -169,3 +169,38 @@ def test_staged_import_still_exact(staged):
         assert np.array_equal(out.reshape(N, M), O.oracle_gemm(A, B, 2, 3, False, True))
     finally:
         deallocGEMMContext(ctx)
+
+
+def test_staged_host_import_mode(lib):
+    """gbs_set_host_import(GBS_HOST_IMPORT_STAGED): host sources (pinned and pageable) go through the
+    copy-engine staging path of this context only; same planes and results as reading in place, and
+    as the oracle; unknown modes are refused."""
+    import torch
+    M, K, N = 300, 1000, 260
+    A = datagen.operand(datagen.SEED_BASE + 2300, M, K, 3, "u")
+    B = datagen.operand(datagen.SEED_BASE + 2301, N, K, 2, "s")
+    want = O.oracle_gemm(A, B, 3, 2, False, True)
+    got = {}
+    for mode in (_capi.GBS_HOST_IMPORT_AUTO, _capi.GBS_HOST_IMPORT_STAGED):
+        for kind in ("pageable", "pinned"):
+            ctx = allocGEMMContext(M, K, N, 3, 2, False, True)
+            try:
+                ctx.set_host_import(mode)
+                a = A if kind == "pageable" else torch.from_numpy(A).pin_memory()
+                b = B if kind == "pageable" else torch.from_numpy(B).pin_memory()
+                ctx.lhs.importRegular(a)
+                ctx.rhs.importRegular(b)
+                gemmBitSerial(ctx)
+                assert np.array_equal(ctx.res.reshape(N, M), want), (mode, kind)
+                got[(mode, kind)] = (planes(ctx, 0), planes(ctx, 1))
+            finally:
+                deallocGEMMContext(ctx)
+    ref = got[(_capi.GBS_HOST_IMPORT_AUTO, "pageable")]
+    for key, (pl, pr) in got.items():
+        assert np.array_equal(pl, ref[0]) and np.array_equal(pr, ref[1]), key
+    ctx = allocGEMMContext(8, 64, 8, 1, 1, False, False)
+    try:
+        assert lib.gbs_set_host_import(ctx._h, 2) == _capi.GBS_EINVAL
+        assert lib.gbs_set_host_import(None, 0) == _capi.GBS_EINVAL
+    finally:
+        deallocGEMMContext(ctx)
