@@ -15,9 +15,9 @@
 //    (double buffered).  Thread (tx, ty) owns lhs rows tx + (BM/4)i and rhs
 //    rows ty + (BN/4)j, so consecutive lanes store consecutive results of the
 //    transposed output row.
-//  * gemm_popc_rows: for at most 16 lhs rows, every lhs row x 256 rhs rows
-//    per CTA, one rhs row per thread (popcounts only on real lhs rows, up to
-//    the next power of two).
+//  * gemm_popc_rows: for at most 16 lhs rows, every lhs row x 64-256 rhs rows
+//    per CTA, 1, 2 or 4 threads per rhs row (popcounts on at most 1-4 lhs rows
+//    per thread past M).
 //  * gemm_popc_grouped: persistent; CTAs pull tiles of many independent
 //    problems from a device queue (atomic counter) and run the same tile code
 //    (the three BM x BN classes, the rows tile, or the skinny class).
@@ -182,8 +182,8 @@ __device__ __forceinline__ void popc_tile(const TileArgs &g, uint64_t m0, uint64
 
 // The rows tile: every lhs row of a problem with at most 16 of them x
 // rows_tile_n(M) rhs rows.  TPR threads share one rhs row, each taking MT of
-// the lhs rows (MT * TPR = M rounded up to a power of two), so popcounts are
-// spent on at most that many lhs rows instead of a 16- or 32-row tile's
+// the lhs rows (MT * TPR >= M, MT of 1 to 4), so popcounts are spent on at
+// most that many lhs rows instead of a 16- or 32-row tile's
 // padding (for M = 1 the BM x BN classes do 16x the work), and no thread
 // counts more than 4 lhs rows per word (past that a tile's popcounts, not its
 // loads, set its time).  The pipeline steps over (rhs plane j, K chunk) pairs:
@@ -284,12 +284,17 @@ __device__ __forceinline__ void popc_rows_tile(const TileArgs &g, uint64_t n0, u
   }
 }
 
+// lhs rows per thread x threads per rhs row: the smallest product >= M (3-row
+// buckets for M = 3, 5-6, 9-12), with the threads per row rows_tile_n's
 template <int KC, bool XOR>
 __device__ __forceinline__ void popc_rows_dispatch(const TileArgs &g, uint64_t n0, uint64_t *smem) {
   if (g.M <= 1) popc_rows_tile<1, 1, KC, XOR>(g, n0, smem);
   else if (g.M <= 2) popc_rows_tile<2, 1, KC, XOR>(g, n0, smem);
+  else if (g.M <= 3) popc_rows_tile<3, 1, KC, XOR>(g, n0, smem);
   else if (g.M <= 4) popc_rows_tile<4, 1, KC, XOR>(g, n0, smem);
+  else if (g.M <= 6) popc_rows_tile<3, 2, KC, XOR>(g, n0, smem);
   else if (g.M <= 8) popc_rows_tile<4, 2, KC, XOR>(g, n0, smem);
+  else if (g.M <= 12) popc_rows_tile<3, 4, KC, XOR>(g, n0, smem);
   else popc_rows_tile<4, 4, KC, XOR>(g, n0, smem);
 }
 

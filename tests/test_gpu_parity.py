@@ -146,11 +146,11 @@ def test_odd_and_skinny_shapes(shape):
             assert np.array_equal(gpu_gemm(A, B, wa, wb, sa, sb, pipe=pipe), ref), (shape, wa, ea, wb, eb, pipe)
 
 
-@pytest.mark.parametrize("M", [1, 2, 3, 5, 8, 9, 16])
+@pytest.mark.parametrize("M", [1, 2, 3, 4, 5, 6, 8, 9, 12, 13, 16])
 def test_popc_rows_tile(lib, M):
-    """The CUDA cores' rows tile (at most 16 lhs rows x 256 rhs rows, one rhs row per thread), forced
+    """The CUDA cores' rows tile (at most 16 lhs rows x 64-256 rhs rows, 1-4 threads per rhs row), forced
     (variant 4) and by the built-in rule: every M bucket, odd and even words per row, rhs row counts
-    off the 256-row tile, bipolar x bipolar (XOR), bipolar x regular (row sums), signed, 8-bit planes."""
+    off the tile, bipolar x bipolar (XOR), bipolar x regular (row sums), signed, 8-bit planes."""
     rng = np.random.default_rng(100 + M)
     for (K, N) in [(64 * 37 + 5, 700), (64 * 40, 256), (1000, 513)]:
         for (wa, ea, wb, eb) in [(1, "u", 1, "u"), (1, "b", 1, "b"), (1, "b", 4, "s"), (3, "s", 2, "u"),
