@@ -46,6 +46,9 @@ PIPE_CHOICES = {"auto": 0, "popc": 1, "bmma": 2, "tc": 3, "tc_pairs": 4, "tc_sme
 DEFAULT_WORKLOAD = "gemm_2048x4096x2048_u3s2"
 
 
+E2E_LANES = 4  # host threads (steps in flight) of the end-to-end measurement
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -681,24 +684,24 @@ def run_ours(args):
         deallocGEMMContext(ctx)
 
     # ---- end to end through the C ABI from pinned host buffers.  Every step imports both operands
-    # from host memory (the pack kernels read it over the host link) and stores its result into a
-    # pinned host buffer (gbs_gemm_to); both calls return once the host memory has been read or
-    # written, as the reference's importRegular and gemmBitSerial do.  Serial: one host thread, one
-    # context, one stream.  Two in flight: two host threads, each with its own context, stream and
-    # result buffer, each running half of the steps, so that one thread's result stores overlap the
-    # other's operand reads (the link carries both directions at once); every step still moves all
-    # of its own bytes.
+    # from host memory and stores its result into a pinned host buffer (gbs_gemm_to); both calls
+    # return once the host memory has been read or written, as the reference's importRegular and
+    # gemmBitSerial do.  Serial: one host thread, one context, one stream.  In flight: E2E_LANES host
+    # threads, each with its own context, stream and result buffer, each running its share of the
+    # steps, so that some threads' result stores overlap others' operand reads (the link carries
+    # both directions at once); every step still moves all of its own bytes.  Measured on GB300
+    # (ms per step; copy-engine imports): 1 thread 0.222, 2 threads 0.147, 3 0.129, 4 0.127.
     hA = torch.from_numpy(A).pin_memory()
     hB = torch.from_numpy(B).pin_memory()
-    hR = [torch.empty(M * N, dtype=torch.int32).pin_memory() for _ in range(2)]
-    e2e_ctx = [allocGEMMContext(M, K, N, wA, wB, sA, sB) for _ in range(3)]
-    e2e_streams = [stream, torch.cuda.Stream(device=dev)]
+    hR = [torch.empty(M * N, dtype=torch.int32).pin_memory() for _ in range(E2E_LANES)]
+    e2e_ctx = [allocGEMMContext(M, K, N, wA, wB, sA, sB) for _ in range(1 + E2E_LANES)]
+    e2e_streams = [stream] + [torch.cuda.Stream(device=dev) for _ in range(E2E_LANES - 1)]
     for c in e2e_ctx:
         force(c)
-    # the two-thread contexts import through the copy engines (GBS_HOST_IMPORT_STAGED): the other
+    # the threads' contexts import through the copy engines (GBS_HOST_IMPORT_STAGED): another
     # thread's GEMM holds most SMs while it stores its result, which starves pack kernels that read
-    # host memory themselves (measured 0.150 against 0.188 ms per step); the serial context reads
-    # its sources in place (0.221 against 0.235 ms)
+    # host memory themselves (two threads: 0.147 against 0.187 ms per step); the serial context reads
+    # its sources in place (0.221 against 0.234 ms)
     for c in e2e_ctx[1:]:
         c.set_host_import(_capi.GBS_HOST_IMPORT_STAGED)
 
@@ -747,7 +750,7 @@ def run_ours(args):
         return reduce_max(sec, world, dev), ok
 
     e2e_serial_s, e2e_serial_ok = e2e_time(1)
-    e2e_s, e2e_ok = e2e_time(2)
+    e2e_s, e2e_ok = e2e_time(E2E_LANES)
     clk.__exit__()
     for c in e2e_ctx:
         deallocGEMMContext(c)
@@ -834,9 +837,9 @@ def run_ours(args):
                     "h2d_bytes_per_step": int(A.nbytes + B.nbytes), "d2h_bytes_per_step": int(M * N * 4),
                     "ms_per_step": round(e2e_s * 1e3, 4), "parity": "bit-exact" if e2e_ok else "MISMATCH",
                     "how": "gbs_import x2 from pinned host buffers + gbs_gemm_to a pinned host buffer per step "
-                           "(each call returns once its host memory is read or written); two steps in flight: "
-                           "two host threads, each with its own context (imports through the copy engines, "
-                           "GBS_HOST_IMPORT_STAGED), stream and result buffer; wall clock over all steps",
+                           f"(each call returns once its host memory is read or written); {E2E_LANES} steps in flight: "
+                           f"{E2E_LANES} host threads, each with its own context (imports through the copy "
+                           "engines, GBS_HOST_IMPORT_STAGED), stream and result buffer; wall clock over all steps",
                     "serial": {"value": round(replica_gops(M, K, N, e2e_serial_s, world), 3),
                                "ms_per_step": round(e2e_serial_s * 1e3, 4),
                                "parity": "bit-exact" if e2e_serial_ok else "MISMATCH",
