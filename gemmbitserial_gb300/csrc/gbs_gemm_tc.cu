@@ -1265,7 +1265,7 @@ EncodeTiledFn encode_fn() {
   if (!f) {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess) {
       f = (EncodeTiledFn)p;
       fn.store(f, std::memory_order_relaxed);
