@@ -473,7 +473,7 @@ int gbs_group_split(const gbs_group *g, uint64_t *popc_problems, uint64_t *tc_pr
 }
 
 int gbs_debug_group_tc_kernel(const gbs_group *g) {
-  if (!g) return fail(GBS_EINVAL, "gbs_debug_group_tc_kernel: group is NULL");
+  if (!g) return -fail(GBS_EINVAL, "gbs_debug_group_tc_kernel: group is NULL");  // negative: not a kernel code
   if (!g->tc.ntiles) return 0;
   return g->tc.nibbles ? 2 : 1;
 }

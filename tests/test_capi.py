@@ -51,6 +51,11 @@ def test_null_context_is_rejected(gbs_lib):
     assert gbs_lib.gbs_gemm(None, None) == _capi.GBS_EINVAL
     assert gbs_lib.gbs_import(None, 0, None, 0, 0, None) == _capi.GBS_EINVAL
     assert gbs_lib.gbs_ctx_free(None) == _capi.GBS_OK
+    for mode in (_capi.GBS_HOST_IMPORT_AUTO, _capi.GBS_HOST_IMPORT_STAGED):
+        assert gbs_lib.gbs_set_host_import(None, mode) == _capi.GBS_EINVAL
+    assert b"gbs_set_host_import" in gbs_lib.gbs_last_error()
+    assert gbs_lib.gbs_set_variant(None, 4) == _capi.GBS_EINVAL
+    assert gbs_lib.gbs_debug_group_tc_kernel(None) < 0
 
 
 def test_python_api_fails_loudly_without_library(monkeypatch, tmp_path):
