@@ -47,6 +47,9 @@ DEFAULT_WORKLOAD = "gemm_2048x4096x2048_u3s2"
 
 
 E2E_LANES = 4  # host threads (steps in flight) of the end-to-end measurement
+# device-side hold before the timed loop: ~6 us at 2 GHz per step (the host enqueues a gbs_gemm call in
+# ~4 us) plus ~10 us for the first
+HOLD_CYCLES_PER_STEP, HOLD_CYCLES_FIXED = 12000, 20000
 
 
 def parse():
@@ -652,6 +655,10 @@ def run_ours(args):
     barrier()
     t_wall = time.perf_counter()
     with torch.cuda.stream(stream):
+        # a device-side sleep holds the stream (before the first event, untimed) while the host
+        # enqueues the K launches, so the events time the GPU's back-to-back rate rather than the
+        # host's enqueue of the first launch into an idle GPU (~0.7 us per step at K = 20)
+        torch.cuda._sleep(HOLD_CYCLES_FIXED + HOLD_CYCLES_PER_STEP * args.steps)
         e0.record(stream)
         for i in range(args.steps):
             _capi.check(lib.gbs_gemm(ctxs[i % P]._h, sh))
@@ -829,6 +836,9 @@ def run_ours(args):
                      5: "tcgen05 (smem digits)"}.get(pipe, str(pipe)),
             **({"forced": {"pipe": args.pipe, "variant": args.variant}}
                if args.pipe != "auto" or args.variant != -1 else {}),
+            "timing": "CUDA events around the K back-to-back launches, queued behind an untimed device-side "
+                      "hold so that the host's enqueue is not in the timed region; wall_s_timed_region includes "
+                      "the hold",
             "isolated_launch": {"ms": round(isolated_ms, 5), "gops": round(gops(M, K, N, isolated_ms * 1e-3), 1),
                                 "how": "each launch alone after a 256 MiB L2 flush, CUDA events around it "
                                        "(launch latency included); median of the steps"},
